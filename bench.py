@@ -1,0 +1,363 @@
+"""Benchmark of the fused phase-field LBM update on GB300 (one JSON line on rank 0).
+
+Workload: the rising perturbed bubble:
+  - 128x128x256 cells, periodic in x and y, bounce-back walls in z;
+  - gravity 1e-5, R 16 at z 48, spherical-harmonic modes l = 2..6;
+  - tau 0.7, sigma 0.05, W 4;
+  - FP32 storage, seeded synthetic initial field.
+A step is one lattice update of the whole lattice. Inputs exceed L2: the f and g buffers
+read by one update hold 637 MB.
+
+  value     MLUPS with the state resident in HBM: cells * K / device time of K updates,
+            CUDA events on the solver's stream, max over ranks. An event after every
+            kernel gives the per-kernel times of the same timed region.
+  e2e       the same metric through the C ABI with host buffers, timed on the host:
+            upload of the initial fields from pinned memory, K updates, and a phi read-back
+            every 100 updates (the reference's dump cadence, src/main.cu:184-189).
+  roofline  the fused collide kernel: algorithmic bytes per launch / average launch time,
+            against the measured HBM copy bandwidth.
+  cpu_baseline  the FP64 oracle (a restatement of the reference update) on the host cores.
+
+--impl reference times the reference path on the host cores. The reference has no CPU
+implementation, so that path is the oracle port. --gpus N > 1 runs N independent replicas,
+one per GPU; the path has no exchange step between cases.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "multic-bubble-cuda_gb300"))
+
+METRIC = "MLUPS and % HBM roofline; FP16-store vs FP32 at fixed Laplace-law error"
+SCENARIO, SEED = 2, 1
+# Algorithmic bytes per lattice update: f and g (19 populations each) read once and written
+# once. The collide kernel moves f in and out and g out; the phi kernel moves g in.
+BYTES_PER_LU = {"f32": 304, "f16": 152, "bf16": 152}
+COLLIDE_BYTES_PER_LU = {"f32": 228, "f16": 114, "bf16": 114}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return ws, rank, local
+
+
+def init_dist(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max(dist, value: float, device=None) -> float:
+    """Max over ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if "Active" in v
+                          and "Not" not in v})
+        loaded = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def make_solver(storage: str, device: int):
+    import mcb
+
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED)
+    cfg.storage = mcb.STORAGES[storage]
+    cfg.device = device
+    s = mcb.Solver(cfg)
+    return s, cfg, (phi, ux, uy, uz)
+
+
+def pinned_like(a):
+    import torch
+
+    t = torch.empty(a.size, dtype=torch.float32, pin_memory=True)
+    v = t.numpy()
+    v[:] = a.reshape(-1)
+    return t, v
+
+
+def device_run(storage, device, steps, warmup, dist):
+    """Device-resident timing: K updates, an event after every kernel."""
+    s, cfg, fields = make_solver(storage, device)
+    s.set_fields(*fields)
+    s.step(warmup)
+    s.synchronize()
+    barrier(dist)
+    total, t_phi, t_col = s.step_profiled(steps)
+    s.synchronize()
+    barrier(dist)
+    d = s.diagnostics(allow_nonfinite=True)
+    s.close()
+    return cfg, total, t_phi, t_col, d
+
+
+def e2e_run(device, steps, save=100):
+    """Host-timed run through the C ABI with host buffers."""
+    import mcb
+
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED)
+    cfg.device = device
+    s = mcb.Solver(cfg)
+    keep = [pinned_like(a) for a in (phi, ux, uy, uz)]
+    host = [v for _, v in keep]
+    out_t, out = pinned_like(np.zeros(s.n, np.float32))
+    # warm the graphs and the copy path once (not timed)
+    s.set_fields(*host)
+    s.step(2 * 16 + 2)
+    s.get("phi", out)
+    s.synchronize()
+    t0 = time.perf_counter()
+    s.set_fields(*host)
+    done, reads = 0, 0
+    while done < steps:
+        n = min(save, steps - done)
+        s.step(n)
+        done += n
+        s.get("phi", out)
+        reads += 1
+    t1 = time.perf_counter()
+    s.close()
+    cells = cfg.nx * cfg.ny * cfg.nz
+    return {"value": cells * steps / (t1 - t0) / 1e6, "unit": "MLUPS",
+            "h2d_bytes_per_step": 4 * 4 * cells / steps,
+            "d2h_bytes_per_step": 4 * cells * reads / steps,
+            "note": f"H2D of phi,u from pinned host once; D2H of phi every {save} updates"}
+
+
+def reference_cuda_run(device, steps):
+    """The reference's own kernels (unmodified src/lbm.cu, sm_103a cubin) on the same GPU, at
+    the same cell count (128x128x256, its frozen-shell mode: it has no walls or gravity)."""
+    from oracle.oracle import ReferenceKernels, harness_available
+    import mcb
+
+    if not harness_available():
+        return {"unavailable": "reference cubin not present (built only where the reference "
+                               "checkout exists)"}
+    nx, ny, nz = 128, 128, 256
+    phi = mcb.fill_phi_reference(nx, ny, nz, 16.0, 4.0)
+    rk = ReferenceKernels(nx, ny, nz, 0.7, 0.05, 0.5, device=device)
+    rk.set_phi(phi)
+    rk.run(5)
+    ms = rk.run(steps)
+    rk.close()
+    return {"value": nx * ny * nz * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
+            "config": "128x128x256 frozen-shell mode, one stream, 10 launches per update",
+            "steps": steps}
+
+
+def cpu_baseline(seconds=10.0, threads=None):
+    """FP64 oracle on the host cores: the scenario at half scale (64x64x128)."""
+    import mcb
+    from oracle.oracle import Oracle, threads_available
+
+    threads = threads or os.cpu_count() or 1
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=0.5)
+    o = Oracle.from_config(cfg, threads=threads)
+    o.set_fields(phi, ux, uy, uz)
+    o.step(1)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        o.step(1)
+        n += 1
+    dt = time.perf_counter() - t0
+    cells = cfg.nx * cfg.ny * cfg.nz
+    return {"value": cells * n / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"FP64 oracle, the same scenario at half scale ({cfg.nx}x{cfg.ny}x{cfg.nz}),"
+                      f" {n} updates in {dt:.1f} s"}
+
+
+def traffic_per_launch(cells):
+    """DRAM bytes per collide launch from the committed ncu summary, scaled to the cells."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    try:
+        return float(d["collide_f32_dram_bytes_per_cell"]) * cells
+    except KeyError:
+        return None
+
+
+def run_reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    steps, warmup = args.steps, args.warmup
+    import mcb
+    from oracle.oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=0.5)
+    o = Oracle.from_config(cfg, threads=threads)
+    o.set_fields(phi, ux, uy, uz)
+    o.step(warmup)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    cells = cfg.nx * cfg.ny * cfg.nz
+    v = cells * steps / dt / 1e6
+    sample = (f"FP64 oracle port of the reference update (the reference has no CPU path), "
+              f"scenario at half scale {cfg.nx}x{cfg.ny}x{cfg.nz}, {steps} updates")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": ws,
+        "steps": steps, "warmup": warmup, "ms_per_step": dt * 1e3 / max(steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "rising perturbed bubble, walls z, gravity 1e-5 (half scale "
+                               "sample)", "cells": cells},
+        "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="solver", choices=["solver", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        return
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+
+    import __graft_entry__
+    import mcb
+
+    if not mcb.LIB_PATH.exists():
+        __graft_entry__.build()
+    dist = init_dist(ws, "nccl")
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    with Clocks(local) as clk:
+        cfg, total_ms, phi_ms, col_ms, diag = device_run("f32", local, args.steps, args.warmup,
+                                                         dist)
+    t_max = reduce_max(dist, total_ms, dev)
+    cells = cfg.nx * cfg.ny * cfg.nz
+    value = ws * cells * args.steps / (t_max * 1e-3) / 1e6
+    hbm, peak_kind = peaks()
+    col_avg_s = col_ms * 1e-3 / args.steps
+    achieved = COLLIDE_BYTES_PER_LU["f32"] * cells / col_avg_s / 1e9
+    update_achieved = BYTES_PER_LU["f32"] * cells / (total_ms * 1e-3 / args.steps) / 1e9
+    result = {
+        "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "rising perturbed bubble 128x128x256, walls z, gravity 1e-5, "
+                               "Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 storage",
+                   "cells": cells, "l2": "inputs larger than L2 (f+g 637 MB per update)",
+                   "parallelism": f"replicas x{ws}", "seed": SEED},
+        "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                     "bytes_per_lu": COLLIDE_BYTES_PER_LU["f32"],
+                     "traffic": traffic_per_launch(cells),
+                     "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
+                     "update_bytes_per_lu": BYTES_PER_LU["f32"],
+                     "kernel_ms": {"k_phi": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+        "mass_q30_finite": bool(diag["finite"]),
+    }
+    if rank == 0:
+        _, t16, p16, c16, d16 = device_run("f16", local, args.steps, args.warmup, None)
+        v16 = cells * args.steps / (t16 * 1e-3) / 1e6
+        result["fp16"] = {"value": v16, "unit": "MLUPS", "ratio_vs_f32": v16 / (value / ws),
+                          "frac_update": BYTES_PER_LU["f16"] * cells / (t16 * 1e-3 / args.steps)
+                          / 1e9 / hbm}
+        result["e2e"] = e2e_run(local, args.steps)
+        result["reference_cuda"] = reference_cuda_run(local, min(args.steps, 200))
+        result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        print(json.dumps(result))
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,235 @@
+/*
+ * mcb.h - C ABI of the GB300-native phase-field lattice-Boltzmann bubble solver.
+ *
+ * The library advances two D3Q19 lattices per update, as the reference's step loop does
+ * (src/main.cu:74-190 of kreeyto/MULTIC-BUBBLE-CUDA):
+ *   - g carries a conservative Allen-Cahn phase field phi;
+ *   - f carries the flow, with regularized collision and He-style surface-tension forcing.
+ * The ten launches of that loop (src/lbm.cu:5-461) become two fused sm_103a kernels per
+ * update. The first pull-streams g and sums phi. The second computes normals, curvature,
+ * force, moments, the regularized f collision and the g collision.
+ *
+ * Conventions:
+ *   - Every call returns an int status: MCB_OK (0) or one of MCB_ERR_*. The reference
+ *     ignores every CUDA return code. mcb_last_error() gives the message of the last
+ *     failure on the calling thread.
+ *   - Fields are float32, nx*ny*nz cells, x fastest: index i + nx*(j + ny*k). This is the
+ *     reference's inline3D (src/header.cuh:22-24) and dump order (src/auxFunctions.cu:49-67).
+ *   - A handle owns all of its device memory (the reference keeps 22 process-global
+ *     arrays, src/var.cu:57-114). Calls on one handle must come from one host thread at a
+ *     time. They are ordered on the handle's own CUDA stream.
+ *   - "Update s" follows the reference's numbering: phi, rho and u of update s are the
+ *     values computed at the start of update s. After mcb_step(h, n) on a fresh handle,
+ *     the fields are those of update n-1. That is what the reference dumps at STEP = n-1.
+ */
+#ifndef MCB_H
+#define MCB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCB_ABI_VERSION 1
+
+/* status codes */
+#define MCB_OK            0
+#define MCB_ERR_INVALID   1  /* bad argument or configuration */
+#define MCB_ERR_CUDA      2  /* a CUDA runtime call failed */
+#define MCB_ERR_ALLOC     3  /* device or host allocation failed */
+#define MCB_ERR_IO        4  /* file could not be written */
+#define MCB_ERR_STATE     5  /* call out of order (e.g. step before fields are set) */
+#define MCB_ERR_NUMERIC   6  /* NaN or Inf found by the diagnostics */
+
+/* boundary handling */
+#define MCB_BC_REF        0  /* the reference's frozen 1-cell shell: rest-equilibrium inflow
+                                (src/lbm.cu:365-401), zero-gradient shell phi lagged by one
+                                update (src/lbm.cu:403-425), shell cells never collide.
+                                Requires g relaxation tau_g = 1 as in src/lbm.cu:290-329. */
+#define MCB_BC_PERIODIC   1  /* periodic in x, y and z */
+#define MCB_BC_WALLS_Z    2  /* periodic in x and y, half-way bounce-back walls at z = -1/2
+                                and z = nz-1/2 (no-slip for f, no-flux for g) */
+
+/* population storage (arithmetic is FP32 in every case) */
+#define MCB_STORE_F32     0  /* f: float32; g: 32-bit fixed point Q2.30 (exact phi mass) */
+#define MCB_STORE_F16     1  /* f, g: float16 deviation form; g rest population Q2.30 */
+#define MCB_STORE_BF16    2  /* f, g: bfloat16 deviation form; g rest population Q2.30 */
+
+/* fields for mcb_get_field */
+#define MCB_FIELD_PHI     0
+#define MCB_FIELD_RHO     1
+#define MCB_FIELD_UX      2
+#define MCB_FIELD_UY      3
+#define MCB_FIELD_UZ      4
+#define MCB_FIELD_P       5  /* p = rho * cs^2, cs^2 = 1/3 */
+
+/* One simulation case. The reference hard-codes these values in src/var.cu:3-25,
+ * src/init.cu:39,46 and src/main.cu:35. */
+typedef struct mcb_config {
+    int   nx, ny, nz;   /* lattice size; each >= 4 (>= 8 for MCB_BC_REF) */
+    int   bc;           /* MCB_BC_* */
+    int   storage;      /* MCB_STORE_* */
+    float tau;          /* f relaxation time; omega = 1/tau (src/var.cu:21-23) */
+    float tau_g;        /* g relaxation time; 1 = full relaxation (src/lbm.cu:290-329) */
+    float sigma;        /* surface tension (src/var.cu:25) */
+    float width;        /* interface width W of the tanh profile */
+    float sharp_c;      /* g sharpening coefficient; <= 0 means (tau_g - 1/2) * 4 / width.
+                           The reference's value is 0.45 (src/var.cu:24). */
+    float gravity;      /* Boussinesq buoyancy: F_z += gravity * (phi - mean phi); 0 = off */
+    int   device;       /* CUDA device ordinal */
+    int   variant;      /* kernel tile variant, -1 = default (see mcb_variant_count) */
+    int   zchunk;       /* z planes per thread block, 0 = default */
+    int   use_graph;    /* 1 = replay updates from a CUDA graph, 0 = plain launches */
+} mcb_config;
+
+/* FP64 diagnostics, reduced on the device in a fixed order (deterministic). */
+typedef struct mcb_diag {
+    double  mass;         /* sum of phi over the lattice (interior only for MCB_BC_REF) */
+    int64_t mass_q30;     /* the same sum as an exact Q2.30 integer */
+    double  kinetic;      /* sum of 0.5 * rho * |u|^2 */
+    double  umax;         /* max |u| */
+    double  rho_in;       /* mean rho over cells with phi > 0.99 */
+    double  rho_out;      /* mean rho over cells with phi < 0.01 */
+    double  dp;           /* cs^2 * (rho_in - rho_out), the Laplace pressure jump */
+    double  n_in, n_out;  /* cell counts of the two averages */
+    double  vol_half;     /* number of cells with phi > 0.5 */
+    double  phi_min, phi_max;
+    int     finite;       /* 1 if every phi, rho and u was finite */
+    int     update;       /* index of the update these values belong to */
+} mcb_diag;
+
+typedef struct mcb_handle mcb_handle;
+typedef struct mcb_batch  mcb_batch;
+
+/* Error text of the last failed call on this thread ("" if none). */
+const char* mcb_last_error(void);
+int  mcb_abi_version(void);
+
+/* Fills cfg with the reference's constants: 64x64x256 (src/var.cu:3-4), tau 0.505,
+ * sigma 0.1, sharp_c 0.45 (src/var.cu:21-25), tau_g 1, width 3 (src/init.cu:46),
+ * MCB_BC_REF, MCB_STORE_F32. */
+int  mcb_config_default(mcb_config* cfg);
+
+/* Replaces initializeVars (src/var.cu:57-114): validates cfg, allocates every device
+ * buffer of one case and creates the handle's stream. */
+int  mcb_create(const mcb_config* cfg, mcb_handle** out);
+int  mcb_destroy(mcb_handle* h);
+
+/* Replaces initTensor/initPhase/initDist (src/init.cu:3-80). phi, ux, uy, uz are host
+ * arrays of nx*ny*nz floats; ux/uy/uz may all be NULL (fluid at rest). rho starts at 1,
+ * f at the second-order equilibrium of (rho, u), g at W_l*phi*(1 + 3 c_l.u). With
+ * u = 0 these are the reference's f = W*rho and g = W*phi. Resets the update counter. */
+int  mcb_set_fields(mcb_handle* h, const float* phi, const float* ux, const float* uy,
+                    const float* uz);
+
+/* Replaces one pass of the step loop body (src/main.cu:77-182), nsteps times.
+ * Asynchronous on the handle's stream; the next mcb_get_field/mcb_diagnostics waits. */
+int  mcb_step(mcb_handle* h, int nsteps);
+int  mcb_synchronize(mcb_handle* h);
+
+/* Copies one field of the latest update to a host array of nx*ny*nz floats. For
+ * MCB_BC_REF the shell of phi holds the zero-gradient copy, as in the reference's dumps. */
+int  mcb_get_field(mcb_handle* h, int which, float* host);
+
+/* FP64 reductions over the latest update (replaces the placeholders of
+ * src/auxFunctions.cu:24-40). Returns MCB_ERR_NUMERIC, with out filled, if a value is
+ * not finite. */
+int  mcb_diagnostics(mcb_handle* h, mcb_diag* out);
+
+/* Replaces copyAndSaveToBinary (src/auxFunctions.cu:49-67): writes phi of the latest
+ * update to "<dir><id>_phi%06d.bin" as raw little-endian float32, nx*ny*nz values,
+ * x fastest. post/fileTreat.py reads the file back. dir must end in a path separator,
+ * as SIM_DIR does in src/main.cu:20-21. */
+int  mcb_dump_phi(mcb_handle* h, const char* dir, const char* id, int step);
+
+/* Replaces generateSimulationInfoFile (src/auxFunctions.cu:12-47): writes
+ * "<dir><id>_info.txt" in the layout post/fileTreat.py:37-124 parses, with
+ * "Precision: float" (the dump format). Measured MLUPS is written when mlups > 0. */
+int  mcb_write_info(const mcb_handle* h, const char* dir, const char* id,
+                    const char* velocity_set, int save_every, int nsteps, double mlups);
+
+/* The two writers behind mcb_dump_phi and mcb_write_info, for host data (no GPU needed).
+ * mcb_write_phi_file writes n floats to "<dir><id>_<name>%06d.bin"
+ * (copyAndSaveToBinary, src/auxFunctions.cu:49-67). mcb_write_info_file writes the
+ * info file of generateSimulationInfoFile (src/auxFunctions.cu:12-47). */
+int  mcb_write_phi_file(const char* dir, const char* id, const char* name, int step,
+                        const float* data, size_t n);
+int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_set,
+                         int nx, int ny, int nz, double tau, double umax, double fx,
+                         double fy, double fz, int save_every, int nsteps, double mlups);
+
+/* Number of updates run since mcb_set_fields, and the size of one case. */
+int  mcb_get_update(const mcb_handle* h, int* update);
+int  mcb_get_dims(const mcb_handle* h, int* nx, int* ny, int* nz);
+
+/* Device time in milliseconds of the last mcb_step call (CUDA events on the handle's
+ * stream around its launches). */
+int  mcb_last_step_ms(mcb_handle* h, float* ms);
+
+/* Like mcb_step, but with plain launches and a CUDA event after every kernel, for
+ * measurement. On return: total_ms is the device time from the first launch to the last;
+ * phi_ms and collide_ms are the summed durations of the two kernels of every update. */
+int  mcb_step_profiled(mcb_handle* h, int nsteps, float* total_ms, float* phi_ms,
+                       float* collide_ms);
+
+/* Kernel tile variants: count and shape (threads in x and y per block). */
+int  mcb_variant_count(void);
+int  mcb_variant_shape(int variant, int* bx, int* by);
+
+/* Times every tile variant and z chunk on a copy of the handle's state for nsteps
+ * updates each. Keeps the fastest variant in the handle, and reports it and its MLUPS.
+ * The handle's fields are restored afterwards. */
+int  mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
+                  double* best_mlups);
+
+/* ---- initial fields (host side; one generator shared by the GPU path and the tests) ---- */
+
+/* One bubble: centre, radius and ellipsoid semi-axis factors (1,1,1 = sphere). */
+typedef struct mcb_bubble {
+    double cx, cy, cz, r;
+    double ax, ay, az;
+} mcb_bubble;
+
+/* The reference's initPhase (src/init.cu:27-49): one bubble of radius r at
+ * (nx/2, ny/2, nz/2), phi = 0.5 + 0.5 tanh(2 (r - |x - c|) / width) in float32 on
+ * interior cells, shell cells 0. */
+int  mcb_fill_phi_reference(int nx, int ny, int nz, float r, float width, float* phi);
+
+/* phi = max over bubbles of 0.5 + 0.5 tanh(2 (R - d) / width). d is the distance to
+ * the centre after dividing each axis offset by the bubble's semi-axis factor. Offsets
+ * take the nearest periodic image in the periodic directions of bc. With MCB_BC_REF the
+ * shell cells are 0, as the reference's init leaves them (src/init.cu:37). */
+int  mcb_fill_phi_bubbles(int nx, int ny, int nz, int bc, float width,
+                          const mcb_bubble* bubbles, int nbubbles, float* phi);
+
+/* Seeded workload generator for the five benchmark scenarios (1..5):
+ *   1 static bubble 64^3; 2 rising perturbed bubble 128x128x256;
+ *   3 32 bubbles 256^3 with velocity noise; 4 one case of the batched set (case_index);
+ *   5 512 bubbles 512^3.
+ * Scale s > 0 multiplies every length (domain, radii, centres) so a scenario can be run
+ * smaller; s = 1 is the full size. Writes cfg, then phi/ux/uy/uz if they are non-NULL
+ * (nx*ny*nz floats each; call once with NULL to learn the size from cfg). All randomness
+ * comes from splitmix64(seed). */
+int  mcb_workload(int scenario, int case_index, uint64_t seed, double scale,
+                  mcb_config* cfg, float* phi, float* ux, float* uy, float* uz);
+
+/* ---- batched cases: many independent cases of uneven size in one launch per phase ---- */
+
+/* All cases must share storage; each keeps its own size, bc, tau, sigma, ... */
+int  mcb_batch_create(const mcb_config* cases, int ncases, mcb_batch** out);
+int  mcb_batch_destroy(mcb_batch* b);
+int  mcb_batch_set_fields(mcb_batch* b, int case_index, const float* phi, const float* ux,
+                          const float* uy, const float* uz);
+int  mcb_batch_step(mcb_batch* b, int nsteps);
+int  mcb_batch_get_field(mcb_batch* b, int case_index, int which, float* host);
+int  mcb_batch_diagnostics(mcb_batch* b, int case_index, mcb_diag* out);
+int  mcb_batch_last_step_ms(mcb_batch* b, float* ms);
+/* Total lattice cells over all cases (for MLUPS). */
+int  mcb_batch_cells(const mcb_batch* b, int64_t* cells);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCB_H */

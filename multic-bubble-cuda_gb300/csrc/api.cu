@@ -1,0 +1,870 @@
+// C ABI of the solver (include/mcb.h): handle and batch life cycle, stepping, field
+// read-back, diagnostics, dumps and the tile autotuner.
+//
+// Reference counterparts:
+//   - state: src/var.cu:57-114 (initializeVars), src/auxFunctions.cu:4-10 (freeMemory);
+//   - init: src/init.cu:3-80;
+//   - step loop: src/main.cu:74-190;
+//   - output: src/auxFunctions.cu:12-67.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mcb.h"
+#include "lattice.h"
+#include "solver.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define MCB_CU(call)                                                                     \
+  do {                                                                                   \
+    const cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(e_ == cudaErrorMemoryAllocation ? MCB_ERR_ALLOC : MCB_ERR_CUDA,        \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+  } while (0)
+
+#define MCB_TRY(expr)          \
+  do {                         \
+    const int r_ = (expr);     \
+    if (r_ != MCB_OK) return r_; \
+  } while (0)
+
+size_t pop_bytes(int storage) { return storage == mcb::kStF32 ? 4 : 2; }
+
+int validate(const mcb_config& c, int index) {
+  if (c.nx < 4 || c.ny < 4 || c.nz < 4)
+    return fail(MCB_ERR_INVALID, "case %d: lattice %dx%dx%d is below 4 cells per axis", index,
+                c.nx, c.ny, c.nz);
+  const long long n = static_cast<long long>(c.nx) * c.ny * c.nz;
+  if (n > 0x7fffffffLL)
+    return fail(MCB_ERR_INVALID, "case %d: %lld cells exceed 2^31-1 per case", index, n);
+  if (c.bc != MCB_BC_REF && c.bc != MCB_BC_PERIODIC && c.bc != MCB_BC_WALLS_Z)
+    return fail(MCB_ERR_INVALID, "case %d: unknown boundary mode %d", index, c.bc);
+  if (c.bc == MCB_BC_REF && (c.nx < 8 || c.ny < 8 || c.nz < 8))
+    return fail(MCB_ERR_INVALID, "case %d: reference boundary mode needs >= 8 cells per axis",
+                index);
+  if (c.storage != MCB_STORE_F32 && c.storage != MCB_STORE_F16 && c.storage != MCB_STORE_BF16)
+    return fail(MCB_ERR_INVALID, "case %d: unknown storage %d", index, c.storage);
+  if (!(c.tau > 0.5f) || !std::isfinite(c.tau))
+    return fail(MCB_ERR_INVALID, "case %d: tau must be > 0.5 (got %g)", index, c.tau);
+  if (!(c.tau_g > 0.5f) || !std::isfinite(c.tau_g))
+    return fail(MCB_ERR_INVALID, "case %d: tau_g must be > 0.5 (got %g)", index, c.tau_g);
+  if (c.bc == MCB_BC_REF && c.tau_g != 1.0f)
+    return fail(MCB_ERR_INVALID,
+                "case %d: reference boundary mode relaxes g fully; tau_g must be 1", index);
+  if (!(c.width > 0.f) || !std::isfinite(c.width))
+    return fail(MCB_ERR_INVALID, "case %d: width must be > 0", index);
+  if (!std::isfinite(c.sigma) || !std::isfinite(c.gravity) || !std::isfinite(c.sharp_c))
+    return fail(MCB_ERR_INVALID, "case %d: non-finite parameter", index);
+  if (c.variant < -1 || c.variant >= mcb::kNumVariants)
+    return fail(MCB_ERR_INVALID, "case %d: variant %d out of range", index, c.variant);
+  if (c.zchunk < 0) return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= 0", index);
+  return MCB_OK;
+}
+
+float sharp_of(const mcb_config& c) {
+  return c.sharp_c > 0.f ? c.sharp_c : (c.tau_g - 0.5f) * 4.0f / c.width;
+}
+
+}  // namespace
+
+// One set of device buffers holding one or more cases.
+struct Solver {
+  int storage = 0, variant = 0, zchunk_req = 0, use_graph = 1, device = 0;
+  std::vector<mcb_config> cfg;
+  std::vector<mcb::CaseDesc> cases;
+  long long cells_total = 0, max_cells = 0;
+  bool bgk = false;
+  mcb::CaseDesc* d_cases = nullptr;
+  void* f[2] = {nullptr, nullptr};
+  void* g[2] = {nullptr, nullptr};
+  int* rest[2] = {nullptr, nullptr};
+  int* p[2] = {nullptr, nullptr};
+  float* macros = nullptr;
+  float* stage = nullptr;
+  mcb::DiagPartial* partials = nullptr;
+  mcb::DiagPartial* result = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_steps = 16;
+  int ntiles = 0, zchunk = 16;
+  int parity = 0, first = 1, latest_p = 1;
+  long long update = -1;
+  std::vector<char> fields_set;
+  std::vector<cudaEvent_t> prof_events;
+  bool stepped = false, timed = false;
+
+  int set_device() {
+    MCB_CU(cudaSetDevice(device));
+    return MCB_OK;
+  }
+
+  void drop_graphs() {
+    for (auto& ge : graph)
+      if (ge) {
+        cudaGraphExecDestroy(ge);
+        ge = nullptr;
+      }
+  }
+
+  void release() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graphs();
+    for (int i = 0; i < 2; ++i) {
+      cudaFree(f[i]);
+      cudaFree(g[i]);
+      cudaFree(rest[i]);
+      cudaFree(p[i]);
+      f[i] = g[i] = nullptr;
+      rest[i] = p[i] = nullptr;
+    }
+    cudaFree(macros);
+    cudaFree(stage);
+    cudaFree(partials);
+    cudaFree(result);
+    cudaFree(d_cases);
+    macros = stage = nullptr;
+    partials = result = nullptr;
+    d_cases = nullptr;
+    for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
+    prof_events.clear();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+    ev0 = ev1 = nullptr;
+    stream = nullptr;
+  }
+
+  // Tile decomposition of every case for the current variant and z chunk.
+  int build_tiles() {
+    const mcb::Variant v = mcb::kVariants[variant];
+    auto tiles_for = [&](int zc) {
+      long long total = 0;
+      for (auto& c : cfg)
+        total += static_cast<long long>((c.nx + v.bx - 1) / v.bx) * ((c.ny + v.by - 1) / v.by) *
+                 ((c.nz + zc - 1) / zc);
+      return total;
+    };
+    int zc = zchunk_req;
+    if (zc <= 0) {
+      // Aim for at least four waves of two blocks per SM on 152 SMs.
+      zc = 32;
+      while (zc > 4 && tiles_for(zc) < 4LL * 2 * 152) zc /= 2;
+    }
+    const long long total = tiles_for(zc);
+    if (total > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tiles (%lld)", total);
+    zchunk = zc;
+    int tile0 = 0;
+    for (size_t i = 0; i < cases.size(); ++i) {
+      mcb::CaseDesc& d = cases[i];
+      d.tiles_x = (d.nx + v.bx - 1) / v.bx;
+      d.tiles_y = (d.ny + v.by - 1) / v.by;
+      d.zchunk = zc;
+      d.tiles_z = (d.nz + zc - 1) / zc;
+      d.tile0 = tile0;
+      tile0 += d.tiles_x * d.tiles_y * d.tiles_z;
+    }
+    ntiles = tile0;
+    drop_graphs();
+    MCB_CU(cudaMemcpyAsync(d_cases, cases.data(), sizeof(mcb::CaseDesc) * cases.size(),
+                           cudaMemcpyHostToDevice, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    return MCB_OK;
+  }
+
+  int create(const mcb_config* cs, int n) {
+    if (!cs || n <= 0) return fail(MCB_ERR_INVALID, "no cases");
+    for (int i = 0; i < n; ++i) MCB_TRY(validate(cs[i], i));
+    storage = cs[0].storage;
+    device = cs[0].device;
+    for (int i = 1; i < n; ++i)
+      if (cs[i].storage != storage || cs[i].device != device)
+        return fail(MCB_ERR_INVALID, "all cases of a batch must share storage and device");
+    variant = cs[0].variant < 0 ? 0 : cs[0].variant;
+    zchunk_req = cs[0].zchunk;
+    use_graph = cs[0].use_graph;
+    cfg.assign(cs, cs + n);
+    cases.resize(n);
+    long long off = 0;
+    for (int i = 0; i < n; ++i) {
+      const mcb_config& c = cs[i];
+      mcb::CaseDesc& d = cases[i];
+      std::memset(&d, 0, sizeof d);
+      d.nx = c.nx;
+      d.ny = c.ny;
+      d.nz = c.nz;
+      d.bc = c.bc;
+      d.ncell = static_cast<long long>(c.nx) * c.ny * c.nz;
+      d.cell_off = off;
+      d.f_off = off * 19;
+      d.g_off = off * 18;
+      d.omega = 1.0f / c.tau;
+      d.omega_g = 1.0f / c.tau_g;
+      d.sigma = c.sigma;
+      d.sharp_c = sharp_of(c);
+      d.gravity = c.gravity;
+      d.phi_mean = 0.f;
+      off += d.ncell;
+      max_cells = std::max(max_cells, d.ncell);
+      if (c.tau_g != 1.0f) bgk = true;
+    }
+    cells_total = off;
+    fields_set.assign(n, 0);
+    MCB_TRY(set_device());
+    MCB_CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    MCB_CU(cudaEventCreate(&ev0));
+    MCB_CU(cudaEventCreate(&ev1));
+    const size_t fb = static_cast<size_t>(cells_total) * 19 * pop_bytes(storage);
+    const size_t gb = static_cast<size_t>(cells_total) * 18 * pop_bytes(storage);
+    const size_t cb = static_cast<size_t>(cells_total) * sizeof(int);
+    for (int i = 0; i < 2; ++i) {
+      MCB_CU(cudaMalloc(&f[i], fb));
+      MCB_CU(cudaMalloc(&g[i], gb));
+      MCB_CU(cudaMalloc(&rest[i], cb));
+      MCB_CU(cudaMalloc(&p[i], cb));
+    }
+    MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
+    MCB_CU(cudaMalloc(&stage, static_cast<size_t>(max_cells) * 4 * sizeof(float)));
+    MCB_CU(cudaMalloc(&partials, sizeof(mcb::DiagPartial) * mcb::kDiagBlocks));
+    MCB_CU(cudaMalloc(&result, sizeof(mcb::DiagPartial)));
+    MCB_CU(cudaMalloc(&d_cases, sizeof(mcb::CaseDesc) * n));
+    return build_tiles();
+  }
+
+  int set_fields(int ci, const float* phi, const float* ux, const float* uy, const float* uz) {
+    if (ci < 0 || ci >= static_cast<int>(cases.size()))
+      return fail(MCB_ERR_INVALID, "case index %d out of range", ci);
+    if (!phi) return fail(MCB_ERR_INVALID, "phi is NULL");
+    const bool has_u = ux || uy || uz;
+    if (has_u && !(ux && uy && uz))
+      return fail(MCB_ERR_INVALID, "ux, uy, uz must be all NULL or all non-NULL");
+    if (stepped && cases.size() > 1)
+      return fail(MCB_ERR_STATE, "batch fields can only be set before the first step");
+    MCB_TRY(set_device());
+    mcb::CaseDesc& d = cases[ci];
+    const size_t n = static_cast<size_t>(d.ncell);
+    double sum = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      if (!std::isfinite(phi[i])) return fail(MCB_ERR_INVALID, "phi[%zu] is not finite", i);
+      sum += phi[i];
+    }
+    d.phi_mean = static_cast<float>(sum / static_cast<double>(n));
+    MCB_CU(cudaMemcpyAsync(stage, phi, n * sizeof(float), cudaMemcpyHostToDevice, stream));
+    if (has_u) {
+      MCB_CU(cudaMemcpyAsync(stage + n, ux, n * sizeof(float), cudaMemcpyHostToDevice, stream));
+      MCB_CU(cudaMemcpyAsync(stage + 2 * n, uy, n * sizeof(float), cudaMemcpyHostToDevice,
+                             stream));
+      MCB_CU(cudaMemcpyAsync(stage + 3 * n, uz, n * sizeof(float), cudaMemcpyHostToDevice,
+                             stream));
+    }
+    MCB_CU(cudaMemcpyAsync(d_cases + ci, &d, sizeof d, cudaMemcpyHostToDevice, stream));
+    // A single case restarts from update 0 in buffer set 0.
+    if (cases.size() == 1 || !stepped) {
+      parity = 0;
+      first = 1;
+      latest_p = 1;
+      update = -1;
+      stepped = false;
+    }
+    mcb::InitArgs a{};
+    a.cases = d_cases;
+    a.case_index = ci;
+    a.phi = stage;
+    a.ux = has_u ? stage + n : nullptr;
+    a.uy = has_u ? stage + 2 * n : nullptr;
+    a.uz = has_u ? stage + 3 * n : nullptr;
+    a.f0 = f[0];
+    a.f1 = f[1];
+    a.g0 = g[0];
+    a.rest0 = rest[0];
+    a.p0 = p[0];
+    a.p1 = p[1];
+    a.macros = macros;
+    a.cells_total = cells_total;
+    MCB_CU(mcb::launch_init(storage, a, d.nx, d.ny, d.nz, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    fields_set[ci] = 1;
+    return MCB_OK;
+  }
+
+  mcb::StepArgs args(bool with_macros) const {
+    mcb::StepArgs a{};
+    a.cases = d_cases;
+    a.ncases = static_cast<int>(cases.size());
+    a.ntiles = ntiles;
+    a.f_in = f[parity];
+    a.f_out = f[parity ^ 1];
+    a.g_in = g[parity];
+    a.g_out = g[parity ^ 1];
+    a.rest_in = rest[parity];
+    a.rest_out = rest[parity ^ 1];
+    a.p_prev = p[parity ^ 1];
+    a.p_cur = p[parity];
+    a.macros = with_macros ? macros : nullptr;
+    a.cells_total = cells_total;
+    a.first = first;
+    return a;
+  }
+
+  int launch_update(bool with_macros) {
+    const mcb::StepArgs a = args(with_macros);
+    MCB_CU(mcb::launch_phi(storage, variant, a, stream));
+    MCB_CU(mcb::launch_collide(storage, variant, bgk, a, stream));
+    latest_p = parity;
+    parity ^= 1;
+    first = 0;
+    ++update;
+    return MCB_OK;
+  }
+
+  // A graph of graph_steps updates (even) starting from buffer set `par`.
+  int ensure_graph(int par) {
+    if (graph[par]) return MCB_OK;
+    const int save_par = parity, save_first = first, save_latest = latest_p;
+    const long long save_update = update;
+    parity = par;
+    first = 0;
+    cudaGraph_t gr = nullptr;
+    MCB_CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = MCB_OK;
+    for (int i = 0; i < graph_steps && rc == MCB_OK; ++i) rc = launch_update(false);
+    const cudaError_t ec = cudaStreamEndCapture(stream, &gr);
+    parity = save_par;
+    first = save_first;
+    latest_p = save_latest;
+    update = save_update;
+    if (rc != MCB_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return rc;
+    }
+    if (ec != cudaSuccess)
+      return fail(MCB_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&graph[par], gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess)
+      return fail(MCB_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
+    return MCB_OK;
+  }
+
+  int step(int nsteps) {
+    if (nsteps < 0) return fail(MCB_ERR_INVALID, "nsteps must be >= 0");
+    for (size_t i = 0; i < fields_set.size(); ++i)
+      if (!fields_set[i]) return fail(MCB_ERR_STATE, "fields of case %zu are not set", i);
+    if (nsteps == 0) return MCB_OK;
+    MCB_TRY(set_device());
+    MCB_CU(cudaEventRecord(ev0, stream));
+    int remaining = nsteps;
+    while (remaining > 0) {
+      const bool eager = first || !use_graph || remaining - 1 < graph_steps;
+      if (eager) {
+        MCB_TRY(launch_update(remaining == 1));
+        --remaining;
+      } else {
+        MCB_TRY(ensure_graph(parity));
+        MCB_CU(cudaGraphLaunch(graph[parity], stream));
+        // The graph leaves the buffer parity unchanged (even length).
+        latest_p = parity ^ 1;
+        update += graph_steps;
+        remaining -= graph_steps;
+      }
+    }
+    MCB_CU(cudaEventRecord(ev1, stream));
+    stepped = true;
+    timed = true;
+    return MCB_OK;
+  }
+
+  // nsteps updates with an event after every kernel: ev[0] | phi ev[2i+1] collide ev[2i+2].
+  int step_profiled(int nsteps, float* total_ms, float* phi_ms, float* collide_ms) {
+    if (nsteps <= 0) return fail(MCB_ERR_INVALID, "nsteps must be > 0");
+    for (size_t i = 0; i < fields_set.size(); ++i)
+      if (!fields_set[i]) return fail(MCB_ERR_STATE, "fields of case %zu are not set", i);
+    MCB_TRY(set_device());
+    const size_t need = 2 * static_cast<size_t>(nsteps) + 1;
+    while (prof_events.size() < need) {
+      cudaEvent_t e;
+      MCB_CU(cudaEventCreate(&e));
+      prof_events.push_back(e);
+    }
+    MCB_CU(cudaEventRecord(prof_events[0], stream));
+    MCB_CU(cudaEventRecord(ev0, stream));
+    for (int i = 0; i < nsteps; ++i) {
+      const mcb::StepArgs a = args(i == nsteps - 1);
+      MCB_CU(mcb::launch_phi(storage, variant, a, stream));
+      MCB_CU(cudaEventRecord(prof_events[2 * i + 1], stream));
+      MCB_CU(mcb::launch_collide(storage, variant, bgk, a, stream));
+      MCB_CU(cudaEventRecord(prof_events[2 * i + 2], stream));
+      latest_p = parity;
+      parity ^= 1;
+      first = 0;
+      ++update;
+    }
+    MCB_CU(cudaEventRecord(ev1, stream));
+    stepped = true;
+    timed = true;
+    MCB_CU(cudaEventSynchronize(ev1));
+    float tp = 0.f, tc = 0.f, tt = 0.f;
+    for (int i = 0; i < nsteps; ++i) {
+      float a = 0.f, b = 0.f;
+      MCB_CU(cudaEventElapsedTime(&a, prof_events[2 * i], prof_events[2 * i + 1]));
+      MCB_CU(cudaEventElapsedTime(&b, prof_events[2 * i + 1], prof_events[2 * i + 2]));
+      tp += a;
+      tc += b;
+    }
+    MCB_CU(cudaEventElapsedTime(&tt, prof_events[0], prof_events[2 * nsteps]));
+    if (total_ms) *total_ms = tt;
+    if (phi_ms) *phi_ms = tp;
+    if (collide_ms) *collide_ms = tc;
+    return MCB_OK;
+  }
+
+  int sync() {
+    MCB_TRY(set_device());
+    MCB_CU(cudaStreamSynchronize(stream));
+    return MCB_OK;
+  }
+
+  int get_field(int ci, int which, float* host) {
+    if (ci < 0 || ci >= static_cast<int>(cases.size()))
+      return fail(MCB_ERR_INVALID, "case index %d out of range", ci);
+    if (!host) return fail(MCB_ERR_INVALID, "host pointer is NULL");
+    if (which < MCB_FIELD_PHI || which > MCB_FIELD_P)
+      return fail(MCB_ERR_INVALID, "unknown field %d", which);
+    if (!fields_set[ci]) return fail(MCB_ERR_STATE, "fields of case %d are not set", ci);
+    MCB_TRY(set_device());
+    const mcb::CaseDesc& d = cases[ci];
+    const int slot = which == MCB_FIELD_P ? 1 : which;
+    const float* src = macros + static_cast<size_t>(slot) * cells_total + d.cell_off;
+    MCB_CU(cudaMemcpyAsync(host, src, static_cast<size_t>(d.ncell) * sizeof(float),
+                           cudaMemcpyDeviceToHost, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    const long long n = d.ncell;
+    if (which == MCB_FIELD_P)
+      for (long long i = 0; i < n; ++i) host[i] *= (1.0f / 3.0f);
+    if (which == MCB_FIELD_PHI && d.bc == mcb::kBcRef && update >= 0) {
+      // Zero-gradient shell copy (boundaryConditions, src/lbm.cu:403-425), applied as if
+      // the three face copies ran one after another: every shell cell takes the value of
+      // the nearest interior cell.
+      const int nx = d.nx, ny = d.ny, nz = d.nz;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) {
+            if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1) continue;
+            const int ic = std::min(std::max(i, 1), nx - 2);
+            const int jc = std::min(std::max(j, 1), ny - 2);
+            const int kc = std::min(std::max(k, 1), nz - 2);
+            host[i + nx * (j + static_cast<long long>(ny) * k)] =
+                host[ic + nx * (jc + static_cast<long long>(ny) * kc)];
+          }
+    }
+    return MCB_OK;
+  }
+
+  int diagnostics(int ci, mcb_diag* out) {
+    if (ci < 0 || ci >= static_cast<int>(cases.size()))
+      return fail(MCB_ERR_INVALID, "case index %d out of range", ci);
+    if (!out) return fail(MCB_ERR_INVALID, "out is NULL");
+    if (!fields_set[ci]) return fail(MCB_ERR_STATE, "fields of case %d are not set", ci);
+    MCB_TRY(set_device());
+    mcb::DiagArgs a{};
+    a.cases = d_cases;
+    a.case_index = ci;
+    a.macros = macros;
+    a.p = p[latest_p];
+    a.cells_total = cells_total;
+    a.partials = partials;
+    a.result = result;
+    MCB_CU(mcb::launch_diag(a, stream));
+    mcb::DiagPartial r;
+    MCB_CU(cudaMemcpyAsync(&r, result, sizeof r, cudaMemcpyDeviceToHost, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    std::memset(out, 0, sizeof *out);
+    out->mass = r.mass;
+    out->mass_q30 = r.mass_q30;
+    out->kinetic = r.ke;
+    out->umax = r.umax;
+    out->n_in = r.n_in;
+    out->n_out = r.n_out;
+    out->rho_in = r.n_in > 0 ? r.rho_in / r.n_in : 0.0;
+    out->rho_out = r.n_out > 0 ? r.rho_out / r.n_out : 0.0;
+    out->dp = (r.n_in > 0 && r.n_out > 0) ? (out->rho_in - out->rho_out) / 3.0 : 0.0;
+    out->vol_half = r.vol_half;
+    out->phi_min = r.phi_min;
+    out->phi_max = r.phi_max;
+    out->finite = r.nonfinite == 0;
+    out->update = static_cast<int>(update);
+    if (!out->finite) return fail(MCB_ERR_NUMERIC, "%lld non-finite values", r.nonfinite);
+    return MCB_OK;
+  }
+
+  int last_ms(float* ms) {
+    if (!ms) return fail(MCB_ERR_INVALID, "ms is NULL");
+    if (!timed) return fail(MCB_ERR_STATE, "no step has been timed");
+    MCB_TRY(set_device());
+    MCB_CU(cudaEventSynchronize(ev1));
+    MCB_CU(cudaEventElapsedTime(ms, ev0, ev1));
+    return MCB_OK;
+  }
+};
+
+struct mcb_handle {
+  Solver s;
+};
+struct mcb_batch {
+  Solver s;
+};
+
+extern "C" {
+
+const char* mcb_last_error(void) { return g_err.c_str(); }
+int mcb_abi_version(void) { return MCB_ABI_VERSION; }
+
+int mcb_config_default(mcb_config* c) {
+  if (!c) return fail(MCB_ERR_INVALID, "cfg is NULL");
+  std::memset(c, 0, sizeof *c);
+  c->nx = 64;
+  c->ny = 64;
+  c->nz = 256;
+  c->bc = MCB_BC_REF;
+  c->storage = MCB_STORE_F32;
+  c->tau = 0.505f;
+  c->tau_g = 1.0f;
+  c->sigma = 0.1f;
+  c->width = 3.0f;
+  c->sharp_c = 0.15f * 3.0f;
+  c->gravity = 0.0f;
+  c->device = 0;
+  c->variant = -1;
+  c->zchunk = 0;
+  c->use_graph = 1;
+  return MCB_OK;
+}
+
+int mcb_create(const mcb_config* cfg, mcb_handle** out) {
+  if (!out) return fail(MCB_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!cfg) return fail(MCB_ERR_INVALID, "cfg is NULL");
+  mcb_handle* h = new (std::nothrow) mcb_handle;
+  if (!h) return fail(MCB_ERR_ALLOC, "host allocation failed");
+  const int rc = h->s.create(cfg, 1);
+  if (rc != MCB_OK) {
+    h->s.release();
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return MCB_OK;
+}
+
+int mcb_destroy(mcb_handle* h) {
+  if (!h) return MCB_OK;
+  cudaSetDevice(h->s.device);
+  h->s.release();
+  delete h;
+  return MCB_OK;
+}
+
+int mcb_set_fields(mcb_handle* h, const float* phi, const float* ux, const float* uy,
+                   const float* uz) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.set_fields(0, phi, ux, uy, uz);
+}
+
+int mcb_step(mcb_handle* h, int nsteps) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.step(nsteps);
+}
+
+int mcb_synchronize(mcb_handle* h) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.sync();
+}
+
+int mcb_get_field(mcb_handle* h, int which, float* host) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.get_field(0, which, host);
+}
+
+int mcb_diagnostics(mcb_handle* h, mcb_diag* out) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.diagnostics(0, out);
+}
+
+int mcb_write_phi_file(const char* dir, const char* id, const char* name, int step,
+                       const float* data, size_t n) {
+  if (!dir || !id || !name || (!data && n)) return fail(MCB_ERR_INVALID, "NULL argument");
+  if (step < 0) return fail(MCB_ERR_INVALID, "step must be >= 0");
+  char tail[64];
+  std::snprintf(tail, sizeof tail, "%06d.bin", step);
+  const std::string path = std::string(dir) + id + "_" + name + tail;
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) return fail(MCB_ERR_IO, "cannot open %s for writing", path.c_str());
+  const size_t w = n ? std::fwrite(data, sizeof(float), n, fp) : 0;
+  const int cl = std::fclose(fp);
+  if (w != n || cl != 0) return fail(MCB_ERR_IO, "short write to %s", path.c_str());
+  return MCB_OK;
+}
+
+int mcb_write_info_file(const char* dir, const char* id, const char* velocity_set, int nx,
+                        int ny, int nz, double tau, double umax, double fx, double fy,
+                        double fz, int save_every, int nsteps, double mlups) {
+  if (!dir || !id || !velocity_set) return fail(MCB_ERR_INVALID, "NULL argument");
+  const std::string path = std::string(dir) + id + "_info.txt";
+  FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) return fail(MCB_ERR_IO, "cannot open %s for writing", path.c_str());
+  // One "key: value" line per item, the value last on its line: post/fileTreat.py:37-124
+  // splits each line on spaces and takes the last token.
+  const char* pad = "                           ";
+  std::fprintf(fp, "---------------------------- SIMULATION INFORMATION ----------------------------\n");
+  std::fprintf(fp, "%sSimulation ID: %s\n", pad, id);
+  std::fprintf(fp, "%sVelocity set: %s\n", pad, velocity_set);
+  std::fprintf(fp, "%sPrecision: float\n", pad);
+  std::fprintf(fp, "%sNX: %d\n", pad, nx);
+  std::fprintf(fp, "%sNY: %d\n", pad, ny);
+  std::fprintf(fp, "%sNZ: %d\n", pad, nz);
+  std::fprintf(fp, "%sNZ_TOTAL: %d\n", pad, nz);
+  std::fprintf(fp, "%sTau: %g\n", pad, tau);
+  std::fprintf(fp, "%sUmax: %e\n", pad, umax);
+  std::fprintf(fp, "%sFX: %e\n", pad, fx);
+  std::fprintf(fp, "%sFY: %e\n", pad, fy);
+  std::fprintf(fp, "%sFZ: %e\n", pad, fz);
+  std::fprintf(fp, "%sSave steps: %d\n", pad, save_every);
+  std::fprintf(fp, "%sNsteps: %d\n", pad, nsteps);
+  std::fprintf(fp, "%sMLUPS: %e\n", pad, mlups > 0 ? mlups : 0.0);
+  std::fprintf(fp, "--------------------------------------------------------------------------------\n");
+  if (std::fclose(fp) != 0) return fail(MCB_ERR_IO, "cannot write %s", path.c_str());
+  return MCB_OK;
+}
+
+int mcb_dump_phi(mcb_handle* h, const char* dir, const char* id, int step) {
+  if (!h || !dir || !id) return fail(MCB_ERR_INVALID, "NULL argument");
+  if (step < 0) return fail(MCB_ERR_INVALID, "step must be >= 0");
+  const mcb::CaseDesc& d = h->s.cases[0];
+  std::vector<float> buf(static_cast<size_t>(d.ncell));
+  MCB_TRY(h->s.get_field(0, MCB_FIELD_PHI, buf.data()));
+  return mcb_write_phi_file(dir, id, "phi", step, buf.data(), buf.size());
+}
+
+int mcb_write_info(const mcb_handle* h, const char* dir, const char* id,
+                   const char* velocity_set, int save_every, int nsteps, double mlups) {
+  if (!h || !dir || !id || !velocity_set) return fail(MCB_ERR_INVALID, "NULL argument");
+  const mcb_config& c = h->s.cfg[0];
+  double umax = 0.0;
+  if (h->s.update >= 0) {
+    mcb_diag dg;
+    if (const_cast<mcb_handle*>(h)->s.diagnostics(0, &dg) == MCB_OK) umax = dg.umax;
+  }
+  return mcb_write_info_file(dir, id, velocity_set, c.nx, c.ny, c.nz, c.tau, umax, 0.0, 0.0,
+                             c.gravity, save_every, nsteps, mlups);
+}
+
+int mcb_get_update(const mcb_handle* h, int* update) {
+  if (!h || !update) return fail(MCB_ERR_INVALID, "NULL argument");
+  *update = static_cast<int>(h->s.update);
+  return MCB_OK;
+}
+
+int mcb_get_dims(const mcb_handle* h, int* nx, int* ny, int* nz) {
+  if (!h || !nx || !ny || !nz) return fail(MCB_ERR_INVALID, "NULL argument");
+  *nx = h->s.cfg[0].nx;
+  *ny = h->s.cfg[0].ny;
+  *nz = h->s.cfg[0].nz;
+  return MCB_OK;
+}
+
+int mcb_last_step_ms(mcb_handle* h, float* ms) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.last_ms(ms);
+}
+
+int mcb_step_profiled(mcb_handle* h, int nsteps, float* total_ms, float* phi_ms,
+                      float* collide_ms) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.step_profiled(nsteps, total_ms, phi_ms, collide_ms);
+}
+
+int mcb_variant_count(void) { return mcb::kNumVariants; }
+
+int mcb_variant_shape(int variant, int* bx, int* by) {
+  if (variant < 0 || variant >= mcb::kNumVariants || !bx || !by)
+    return fail(MCB_ERR_INVALID, "bad variant or NULL argument");
+  *bx = mcb::kVariants[variant].bx;
+  *by = mcb::kVariants[variant].by;
+  return MCB_OK;
+}
+
+int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
+                 double* best_mlups) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  if (nsteps < 2) return fail(MCB_ERR_INVALID, "nsteps must be >= 2");
+  Solver& s = h->s;
+  if (!s.fields_set[0]) return fail(MCB_ERR_STATE, "fields are not set");
+  MCB_TRY(s.set_device());
+  // Save the state the next update reads, so every trial starts from it.
+  const int par = s.parity;
+  const size_t n = static_cast<size_t>(s.cells_total);
+  const size_t fb = n * 19 * pop_bytes(s.storage), gb = n * 18 * pop_bytes(s.storage);
+  void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
+  auto free_all = [&]() {
+    cudaFree(fs);
+    cudaFree(gs);
+    cudaFree(rs);
+    cudaFree(ps);
+    cudaFree(ms);
+  };
+  if (cudaMalloc(&fs, fb) != cudaSuccess || cudaMalloc(&gs, gb) != cudaSuccess ||
+      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 8) != cudaSuccess ||
+      cudaMalloc(&ms, n * 20) != cudaSuccess) {
+    free_all();
+    return fail(MCB_ERR_ALLOC, "autotune: no room for a state copy");
+  }
+  const int save_first = s.first, save_latest = s.latest_p, save_variant = s.variant;
+  const int save_zreq = s.zchunk_req;
+  const long long save_update = s.update;
+  auto snapshot = [&](bool restore) -> int {
+    auto cp = [&](void* dst, const void* src, size_t b) {
+      return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, s.stream);
+    };
+    cudaError_t e = cudaSuccess;
+    if (!restore) {
+      if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
+      if (e == cudaSuccess) e = cp(gs, s.g[par], gb);
+      if (e == cudaSuccess) e = cp(rs, s.rest[par], n * 4);
+      if (e == cudaSuccess) e = cp(ps, s.p[0], n * 4);
+      if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + n * 4, s.p[1], n * 4);
+      if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
+    } else {
+      if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
+      if (e == cudaSuccess) e = cp(s.g[par], gs, gb);
+      if (e == cudaSuccess) e = cp(s.rest[par], rs, n * 4);
+      if (e == cudaSuccess) e = cp(s.p[0], ps, n * 4);
+      if (e == cudaSuccess) e = cp(s.p[1], static_cast<char*>(ps) + n * 4, n * 4);
+      if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);
+      // Reference-mode shells keep f = W_l in both buffers; the other buffer's interior
+      // is rewritten by the next update.
+      if (e == cudaSuccess) e = cp(s.f[par ^ 1], fs, fb);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) return fail(MCB_ERR_CUDA, "autotune copy: %s", cudaGetErrorString(e));
+    s.parity = par;
+    s.first = save_first;
+    s.latest_p = save_latest;
+    s.update = save_update;
+    return MCB_OK;
+  };
+  int rc = snapshot(false);
+  double best = -1.0;
+  int bv = save_variant, bz = s.zchunk;
+  const int zc_list[] = {4, 8, 16, 32, 64};
+  for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
+    for (int zc : zc_list) {
+      if (zc > s.cfg[0].nz) continue;
+      s.variant = v;
+      s.zchunk_req = zc;
+      rc = s.build_tiles();
+      if (rc != MCB_OK) break;
+      rc = s.step(2);  // warm-up (also takes the graph capture out of the timing)
+      if (rc == MCB_OK) rc = s.step(nsteps);
+      float ms = 0.f;
+      if (rc == MCB_OK) rc = s.last_ms(&ms);
+      if (rc != MCB_OK) break;
+      const double mlups = static_cast<double>(s.cells_total) * nsteps / (ms * 1e-3) / 1e6;
+      if (mlups > best) {
+        best = mlups;
+        bv = v;
+        bz = zc;
+      }
+      rc = snapshot(true);
+      if (rc != MCB_OK) break;
+    }
+  }
+  free_all();
+  s.variant = (rc == MCB_OK) ? bv : save_variant;
+  s.zchunk_req = (rc == MCB_OK) ? bz : save_zreq;
+  const int rb = s.build_tiles();
+  if (rc != MCB_OK) return rc;
+  if (rb != MCB_OK) return rb;
+  if (best_variant) *best_variant = bv;
+  if (best_zchunk) *best_zchunk = bz;
+  if (best_mlups) *best_mlups = best;
+  return MCB_OK;
+}
+
+// ---- batch ----
+
+int mcb_batch_create(const mcb_config* cases, int ncases, mcb_batch** out) {
+  if (!out) return fail(MCB_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  mcb_batch* b = new (std::nothrow) mcb_batch;
+  if (!b) return fail(MCB_ERR_ALLOC, "host allocation failed");
+  const int rc = b->s.create(cases, ncases);
+  if (rc != MCB_OK) {
+    b->s.release();
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return MCB_OK;
+}
+
+int mcb_batch_destroy(mcb_batch* b) {
+  if (!b) return MCB_OK;
+  cudaSetDevice(b->s.device);
+  b->s.release();
+  delete b;
+  return MCB_OK;
+}
+
+int mcb_batch_set_fields(mcb_batch* b, int ci, const float* phi, const float* ux,
+                         const float* uy, const float* uz) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  return b->s.set_fields(ci, phi, ux, uy, uz);
+}
+
+int mcb_batch_step(mcb_batch* b, int nsteps) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  return b->s.step(nsteps);
+}
+
+int mcb_batch_get_field(mcb_batch* b, int ci, int which, float* host) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  return b->s.get_field(ci, which, host);
+}
+
+int mcb_batch_diagnostics(mcb_batch* b, int ci, mcb_diag* out) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  return b->s.diagnostics(ci, out);
+}
+
+int mcb_batch_last_step_ms(mcb_batch* b, float* ms) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  return b->s.last_ms(ms);
+}
+
+int mcb_batch_cells(const mcb_batch* b, int64_t* cells) {
+  if (!b || !cells) return fail(MCB_ERR_INVALID, "NULL argument");
+  *cells = b->s.cells_total;
+  return MCB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,716 @@
+// Fused sm_103a kernels of one lattice update.
+//
+// The reference runs ten launches per update (src/main.cu:79-178):
+//   phiCalc, gradCalc, curvatureCalc, momentiCalc, collisionFluid, collisionPhase,
+//   movingWallBC, streamingCalc, fgBoundary, boundaryConditions.
+// Between them it keeps 22 full-grid arrays in HBM. Here one update is two kernels:
+//
+//   k_phi      pull-gathers the 19 g populations of every cell and sums them into phi.
+//              This is streamingCalc + phiCalc (src/lbm.cu:337-357, 5-26), plus the lagged
+//              shell copy of boundaryConditions (src/lbm.cu:403-425) in reference mode.
+//   k_collide  marches a BX x BY column of cells through a z chunk. It keeps a 5-plane
+//              ring of phi (halo 2) and a 3-plane ring of normals (halo 1) in shared
+//              memory. For every cell it computes:
+//                - the isotropic normals and |grad phi| (gradCalc, src/lbm.cu:34-72);
+//                - the curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125);
+//                - the moments (momentiCalc, src/lbm.cu:133-225);
+//                - the regularized f collision with He forcing (collisionFluid,
+//                  src/lbm.cu:233-288);
+//                - the g collision (collisionPhase, src/lbm.cu:290-329).
+//              Populations are stored post-collision at the colliding cell. The next
+//              update gathers them from x - c_l (pull streaming). In reference mode the
+//              shell cells write the rest-equilibrium inflow of fgBoundary
+//              (src/lbm.cu:365-401).
+//
+// HBM traffic per lattice update: f and g are read once and written once, plus 8 bytes
+// of phi. Nothing else reaches HBM: normals, curvature, force and moments live in
+// registers and shared memory.
+//
+// phi is carried as Q2.30 fixed point. Every g collision writes the rest population as
+// the exact integer remainder. The 19 stored values of a cell therefore add up to its
+// phi exactly, and streaming and bounce-back are permutations. So the lattice sum of
+// phi is invariant to the last bit in periodic and walled domains.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cfloat>
+
+#include "lattice.h"
+#include "solver.h"
+
+namespace mcb {
+namespace {
+
+// ------------------------------------------------------------------ storage policies --
+
+// f float32 absolute, g Q2.30 absolute (32-bit storage).
+struct StF32 {
+  using FT = float;
+  using GT = int;
+  static constexpr bool kDev = false;
+  static __device__ __forceinline__ float fload(const FT* p) { return __ldg(p); }
+  static __device__ __forceinline__ GT gload(const GT* p) { return __ldg(p); }
+  template <int L> static __device__ __forceinline__ float f_dec(FT v) { return v; }
+  template <int L> static __device__ __forceinline__ FT f_enc(float f) { return f; }
+  template <int L> static __device__ __forceinline__ int g_dec(GT v, int) { return v; }
+  template <int L>
+  static __device__ __forceinline__ GT g_enc(float g, int, int& q) {
+    q = __float2int_rn(g * kQ30);
+    return q;
+  }
+  template <int L> static __device__ __forceinline__ GT g_shell(int p) { return wsplit<L>(p); }
+  static __device__ __forceinline__ int rest_store(int p, int sumq) { return p - sumq; }
+  static __device__ __forceinline__ int rest_dec(int stored, int) { return stored; }
+  static __device__ __forceinline__ int rest_shell(int p) { return wsplit_rest(p); }
+  static __device__ __forceinline__ int rest_init(float g0, int) {
+    return __float2int_rn(g0 * kQ30);
+  }
+};
+
+struct HalfOps {
+  using T = __half;
+  static __device__ __forceinline__ float tof(T v) { return __half2float(v); }
+  static __device__ __forceinline__ T fromf(float f) { return __float2half_rn(f); }
+  // Every finite half is a multiple of 2^-24, hence an exact Q2.30 integer.
+  static __device__ __forceinline__ T enc_exact(float d) {
+    return __float2half_rn(fminf(fmaxf(d, -1.875f), 1.875f));
+  }
+};
+
+struct Bf16Ops {
+  using T = __nv_bfloat16;
+  static __device__ __forceinline__ float tof(T v) { return __bfloat162float(v); }
+  static __device__ __forceinline__ T fromf(float f) { return __float2bfloat16_rn(f); }
+  // bfloat16 values below 2^-22 are not multiples of 2^-30. Small deviations are therefore
+  // rounded to k * 2^-30 with |k| <= 256 first; that value is exact in bfloat16. Larger
+  // ones round to a multiple of 2^-29.
+  static __device__ __forceinline__ T enc_exact(float d) {
+    d = fminf(fmaxf(d, -1.875f), 1.875f);
+    const int k = __float2int_rn(d * kQ30);
+    if (k <= 256 && k >= -256) return __float2bfloat16_rn(static_cast<float>(k) * kInvQ30);
+    return __float2bfloat16_rn(d);
+  }
+};
+
+// 16-bit deviation form: f_l - W_l, and g_l - w_l(phi of the cell that collided it).
+// w_l is the exact integer split of that phi. The g rest population is a Q2.30 integer
+// holding the exact remainder.
+template <class O>
+struct St16 {
+  using FT = typename O::T;
+  using GT = typename O::T;
+  static constexpr bool kDev = true;
+  static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
+  static __device__ __forceinline__ GT gload(const GT* p) { return __ldg(p); }
+  template <int L> static __device__ __forceinline__ float f_dec(FT v) {
+    return wf(L) + O::tof(v);
+  }
+  template <int L> static __device__ __forceinline__ FT f_enc(float f) {
+    return O::fromf(f - wf(L));
+  }
+  template <int L> static __device__ __forceinline__ int g_dec(GT v, int psrc) {
+    return wsplit<L>(psrc) + __float2int_rn(O::tof(v) * kQ30);
+  }
+  template <int L>
+  static __device__ __forceinline__ GT g_enc(float g, int pself, int& q) {
+    const int w = wsplit<L>(pself);
+    const GT h = O::enc_exact(g - static_cast<float>(w) * kInvQ30);
+    q = w + __float2int_rn(O::tof(h) * kQ30);
+    return h;
+  }
+  template <int L> static __device__ __forceinline__ GT g_shell(int) { return O::fromf(0.0f); }
+  static __device__ __forceinline__ int rest_store(int p, int sumq) {
+    return p - sumq - wsplit_rest(p);
+  }
+  static __device__ __forceinline__ int rest_dec(int stored, int p) {
+    return wsplit_rest(p) + stored;
+  }
+  static __device__ __forceinline__ int rest_shell(int) { return 0; }
+  static __device__ __forceinline__ int rest_init(float g0, int p) {
+    return __float2int_rn(g0 * kQ30) - wsplit_rest(p);
+  }
+};
+
+using StH16 = St16<HalfOps>;
+using StB16 = St16<Bf16Ops>;
+
+// ------------------------------------------------------------------------- helpers --
+
+// Value for the source cell x - c (C = +1 takes the minus neighbour).
+template <int C, class T>
+__device__ __forceinline__ T src_of(T m, T o, T p) {
+  if constexpr (C == 1) return m;
+  else if constexpr (C == -1) return p;
+  else return o;
+}
+// Value for the neighbour x + c.
+template <int C, class T>
+__device__ __forceinline__ T nbr_of(T m, T o, T p) {
+  if constexpr (C == 1) return p;
+  else if constexpr (C == -1) return m;
+  else return o;
+}
+
+__device__ __forceinline__ int wrap1(int v, int n) {
+  return v < 0 ? v + n : (v >= n ? v - n : v);
+}
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+__device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int tile) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&cs[mid].tile0) <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct Tile {
+  int nx, ny, nz, bc, zb, ze, xt, yt;
+  long long ncell, cell_off, f_off, g_off;
+};
+
+template <int BX, int BY>
+__device__ __forceinline__ Tile locate_tile(const StepArgs& a) {
+  const int c = find_case(a.cases, a.ncases, blockIdx.x);
+  const CaseDesc* cd = a.cases + c;
+  Tile t;
+  t.nx = __ldg(&cd->nx);
+  t.ny = __ldg(&cd->ny);
+  t.nz = __ldg(&cd->nz);
+  t.bc = __ldg(&cd->bc);
+  const int tiles_x = __ldg(&cd->tiles_x), tiles_y = __ldg(&cd->tiles_y);
+  const int zchunk = __ldg(&cd->zchunk);
+  int r = static_cast<int>(blockIdx.x) - __ldg(&cd->tile0);
+  t.xt = (r % tiles_x) * BX;
+  r /= tiles_x;
+  t.yt = (r % tiles_y) * BY;
+  t.zb = (r / tiles_y) * zchunk;
+  t.ze = min(t.zb + zchunk, t.nz);
+  t.ncell = __ldg(&cd->ncell);
+  t.cell_off = __ldg(&cd->cell_off);
+  t.f_off = __ldg(&cd->f_off);
+  t.g_off = __ldg(&cd->g_off);
+  return t;
+}
+
+// ---------------------------------------------------------------- k_phi: g -> phi --
+
+template <class S, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY) k_phi(const StepArgs a) {
+  using GT = typename S::GT;
+  const Tile t = locate_tile<BX, BY>(a);
+  const int nx = t.nx, ny = t.ny, nz = t.nz;
+  const int x = t.xt + static_cast<int>(threadIdx.x);
+  const int y = t.yt + static_cast<int>(threadIdx.y);
+  if (x >= nx || y >= ny) return;
+  const long long n = t.ncell;
+  const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
+  const int* __restrict__ rest = a.rest_in + t.cell_off;
+  const int* __restrict__ pprev = a.p_prev + t.cell_off;
+  int* __restrict__ pcur = a.p_cur + t.cell_off;
+  const int nxy = nx * ny;
+  const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
+  const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+  const int ym = (y == 0 ? ny - 1 : y - 1) * nx, yo = y * nx;
+  const int yp = (y == ny - 1 ? 0 : y + 1) * nx;
+  const bool shell_xy = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1);
+
+  for (int z = t.zb; z < t.ze; ++z) {
+    const int zo = z * nxy;
+    const int idx = x + yo + zo;
+    int P;
+    if (ref && (shell_xy || z == 0 || z == nz - 1)) {
+      // Shell: zero-gradient copy of the previous update's interior phi; zero on the
+      // first update (the reference's memset, src/var.cu:86).
+      if (a.first) {
+        P = 0;
+      } else {
+        const int xc = clampi(x, 1, nx - 2), yc = clampi(y, 1, ny - 2);
+        const int zc = clampi(z, 1, nz - 2);
+        P = __ldg(pprev + xc + yc * nx + zc * nxy);
+      }
+    } else {
+      const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
+      const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
+      const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+      const int pself = S::kDev ? __ldg(pprev + idx) : 0;
+      P = S::rest_dec(__ldg(rest + idx), pself);
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr int O = opp(L);
+        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+        if (bounce) {
+          P += S::template g_dec<O>(S::gload(gin + (O - 1) * n + idx), pself);
+        } else {
+          const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                        src_of<cx(L)>(xm, x, xp);
+          const int ps = S::kDev ? __ldg(pprev + s) : 0;
+          P += S::template g_dec<L>(S::gload(gin + (L - 1) * n + s), ps);
+        }
+      });
+    }
+    pcur[idx] = P;
+  }
+}
+
+// ------------------------------------------------------- k_collide: the fused update --
+
+template <class S, bool BGK, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(const StepArgs a) {
+  using FT = typename S::FT;
+  using GT = typename S::GT;
+  constexpr int NT = BX * BY;
+  constexpr int PX = BX + 4, PY = BY + 4, PP = PX * PY;  // phi plane, halo 2
+  constexpr int HX = BX + 2, HY = BY + 2, HP = HX * HY;  // normals plane, halo 1
+  constexpr int KPF = (PP + NT - 1) / NT;                // phi values per thread per plane
+  __shared__ float sphi[5][PP];
+  __shared__ float4 snrm[3][HP];
+
+  const Tile t = locate_tile<BX, BY>(a);
+  const int nx = t.nx, ny = t.ny, nz = t.nz;
+  const int nxy = nx * ny;
+  const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + BX * ty;
+  const int x = t.xt + tx, y = t.yt + ty;
+  const bool active = x < nx && y < ny;
+  const long long n = t.ncell;
+
+  const CaseDesc* cd = a.cases + find_case(a.cases, a.ncases, blockIdx.x);
+  const float omega = __ldg(&cd->omega), omega_g = __ldg(&cd->omega_g);
+  const float sigma = __ldg(&cd->sigma), sharp_c = __ldg(&cd->sharp_c);
+  const float gravity = __ldg(&cd->gravity), phi_mean = __ldg(&cd->phi_mean);
+
+  const int* __restrict__ pcur = a.p_cur + t.cell_off;
+
+  // Halo cells of a phi plane handled by this thread: their in-plane offsets are fixed.
+  int hoff[KPF];
+#pragma unroll
+  for (int k = 0; k < KPF; ++k) {
+    const int i = tid + k * NT;
+    if (i < PP) {
+      int gx = t.xt - 2 + i % PX, gy = t.yt - 2 + i / PX;
+      if (!ref) {
+        gx = wrap1(gx, nx);
+        gy = wrap1(gy, ny);
+      }
+      hoff[k] = clampi(gx, 0, nx - 1) + clampi(gy, 0, ny - 1) * nx;
+    } else {
+      hoff[k] = 0;
+    }
+  }
+  auto zmap = [&](int z) -> int {
+    if (t.bc == kBcPeriodic) z = wrap1(z, nz);
+    else if (walls) z = z < 0 ? -1 - z : (z >= nz ? 2 * nz - 1 - z : z);  // mirror
+    return clampi(z, 0, nz - 1);
+  };
+  int pre[KPF];
+  auto issue = [&](int zpl) {
+    const int* base = pcur + static_cast<long long>(zmap(zpl)) * nxy;
+#pragma unroll
+    for (int k = 0; k < KPF; ++k)
+      if (tid + k * NT < PP) pre[k] = __ldg(base + hoff[k]);
+  };
+  auto commit = [&](int zpl) {
+    float* d = sphi[(zpl + 5) % 5];
+#pragma unroll
+    for (int k = 0; k < KPF; ++k)
+      if (tid + k * NT < PP) d[tid + k * NT] = __int2float_rn(pre[k]) * kInvQ30;
+  };
+  // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72).
+  auto normals = [&](int zp) {
+    const float* pm = sphi[(zp + 4) % 5];
+    const float* p0 = sphi[(zp + 5) % 5];
+    const float* pp = sphi[(zp + 6) % 5];
+    float4* dst = snrm[(zp + 3) % 3];
+    const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
+    for (int i = tid; i < HP; i += NT) {
+      const int hx = i % HX, hy = i / HX;
+      const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+      const bool zero = zshell || (ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1));
+      if (!zero) {
+        const int c = (hy + 1) * PX + hx + 1;
+        float gxs = 0.f, gys = 0.f, gzs = 0.f;
+        static_for<1, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          constexpr float w3 = 3.0f * wf(L);
+          const float v = nbr_of<cz(L)>(pm, p0, pp)[c + cy(L) * PX + cx(L)];
+          if constexpr (cx(L) != 0) gxs += (cx(L) * w3) * v;
+          if constexpr (cy(L) != 0) gys += (cy(L) * w3) * v;
+          if constexpr (cz(L) != 0) gzs += (cz(L) * w3) * v;
+        });
+        const float g2 = gxs * gxs + gys * gys + gzs * gzs;
+        const float fac = rsqrtf(fmaxf(g2, 1e-9f));
+        r = make_float4(gxs * fac, gys * fac, gzs * fac, g2 * fac);
+      }
+      dst[i] = r;
+    }
+  };
+
+  // Per-thread neighbour offsets in x and y (periodic wrap; reference-mode interior cells
+  // never reach past the shell).
+  const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+  const int ym = (y == 0 ? ny - 1 : y - 1) * nx, yo = y * nx;
+  const int yp = (y == ny - 1 ? 0 : y + 1) * nx;
+  const bool shell_xy = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1);
+
+  const FT* __restrict__ fin = static_cast<const FT*>(a.f_in) + t.f_off;
+  FT* __restrict__ fout = static_cast<FT*>(a.f_out) + t.f_off;
+  const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
+  GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
+  const int* __restrict__ rest_in = a.rest_in + t.cell_off;
+  int* __restrict__ rest_out = a.rest_out + t.cell_off;
+  const int* __restrict__ pprev = a.p_prev + t.cell_off;
+
+  // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
+  for (int zpl = t.zb - 2; zpl <= t.zb + 1; ++zpl) {
+    issue(zpl);
+    commit(zpl);
+  }
+  issue(t.zb + 2);
+  __syncthreads();
+  normals(t.zb - 1);
+  normals(t.zb);
+
+  for (int z = t.zb; z < t.ze; ++z) {
+    commit(z + 2);
+    if (z + 3 <= t.ze + 1) issue(z + 3);
+
+    const int zo = z * nxy;
+    const int idx = x + yo + zo;
+    const bool shell = shell_xy || (ref && (z == 0 || z == nz - 1));
+    const bool work = active && !shell;
+    const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
+    const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
+    const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+
+    // Pull the 19 f populations (issued before the barriers to overlap their latency).
+    FT fr[kQ];
+    if (work) {
+      fr[0] = S::fload(fin + idx);
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr int O = opp(L);
+        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+        if (bounce) {
+          fr[L] = S::fload(fin + O * n + idx);
+        } else {
+          const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                        src_of<cx(L)>(xm, x, xp);
+          fr[L] = S::fload(fin + L * n + s);
+        }
+      });
+    }
+    __syncthreads();
+    normals(z + 1);
+    __syncthreads();
+    if (!active) continue;
+
+    const int pc = __ldg(pcur + idx);
+    if (shell) {
+      // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
+      // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        gout[(L - 1) * n + idx] = S::template g_shell<L>(pc);
+      });
+      rest_out[idx] = S::rest_shell(pc);
+      if (a.macros) {
+        const long long T = a.cells_total, o = t.cell_off + idx;
+        a.macros[o] = __int2float_rn(pc) * kInvQ30;
+        a.macros[T + o] = 1.0f;
+        a.macros[2 * T + o] = 0.0f;
+        a.macros[3 * T + o] = 0.0f;
+        a.macros[4 * T + o] = 0.0f;
+      }
+      continue;
+    }
+
+    // Curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125).
+    const float4* nm = snrm[(z + 2) % 3];
+    const float4* n0 = snrm[(z + 3) % 3];
+    const float4* np = snrm[(z + 4) % 3];
+    const int hc = (ty + 1) * HX + tx + 1;
+    const float4 nc = n0[hc];
+    float kap = 0.f;
+    static_for<1, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      constexpr float w3 = 3.0f * wf(L);
+      const float4 nb = nbr_of<cz(L)>(nm, n0, np)[hc + cy(L) * HX + cx(L)];
+      float cn = 0.f;
+      if constexpr (cx(L) != 0) cn += cx(L) * nb.x;
+      if constexpr (cy(L) != 0) cn += cy(L) * nb.y;
+      if constexpr (cz(L) != 0) cn += cz(L) * nb.z;
+      kap -= w3 * cn;
+    });
+    const float phi = sphi[(z + 5) % 5][(ty + 2) * PX + tx + 2];
+    const float mult = sigma * kap;
+    const float Fx = mult * nc.x * nc.w;
+    const float Fy = mult * nc.y * nc.w;
+    float Fz = mult * nc.z * nc.w;
+    if (gravity != 0.f) Fz += gravity * (phi - phi_mean);
+
+    // Moments (momentiCalc, src/lbm.cu:133-225). The non-equilibrium second moment is
+    // sum c c (f - feq + HeF). For the D3Q19 second-order equilibrium its equilibrium
+    // and forcing parts reduce in closed form:
+    //   sum c_a c_b feq = rho (cs^2 d_ab + u_a u_b)
+    //   sum c_a c_b HeF = (u_a F_b + u_b F_a)/2 - 3/2 (u.F) u_a u_b
+    // This uses the 4th-order isotropy of D3Q19.
+    float f[kQ];
+    static_for<0, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      f[L] = S::template f_dec<L>(fr[L]);
+    });
+    float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+    float sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+    static_for<0, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      const float v = f[L];
+      rho += v;
+      if constexpr (cx(L) != 0) { jx += cx(L) * v; sxx += v; }
+      if constexpr (cy(L) != 0) { jy += cy(L) * v; syy += v; }
+      if constexpr (cz(L) != 0) { jz += cz(L) * v; szz += v; }
+      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * v;
+      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
+      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
+    });
+    const float inv_rho = 1.0f / rho;
+    const float ux = (jx + 0.5f * Fx) * inv_rho;
+    const float uy = (jy + 0.5f * Fy) * inv_rho;
+    const float uz = (jz + 0.5f * Fz) * inv_rho;
+    const float uF = ux * Fx + uy * Fy + uz * Fz;
+    const float u2 = ux * ux + uy * uy + uz * uz;
+    const float h = 1.5f * uF;
+    const float pxx = sxx - rho * (1.0f / 3.0f + ux * ux) + ux * Fx - h * ux * ux;
+    const float pyy = syy - rho * (1.0f / 3.0f + uy * uy) + uy * Fy - h * uy * uy;
+    const float pzz = szz - rho * (1.0f / 3.0f + uz * uz) + uz * Fz - h * uz * uz;
+    const float pxy = sxy - rho * ux * uy + 0.5f * (ux * Fy + uy * Fx) - h * ux * uy;
+    const float pxz = sxz - rho * ux * uz + 0.5f * (ux * Fz + uz * Fx) - h * ux * uz;
+    const float pyz = syz - rho * uy * uz + 0.5f * (uy * Fz + uz * Fy) - h * uy * uz;
+    const float tr3 = (pxx + pyy + pzz) * (1.0f / 3.0f);
+
+    // Regularized collision with He forcing (collisionFluid, src/lbm.cu:233-288):
+    //   f*_l = feq_l + (1 - omega) W_l/(2 cs^4) Q_l:Pi + HeF_l
+    //        = W_l [E_l (rho + 3/2 (c_l.F - u.F)) + 9/2 (1 - omega) Q_l:Pi]
+    // with E_l = 1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2. Opposite pairs share Q_l:Pi and flip
+    // c.u and c.F.
+    const float om = (1.0f - omega) * 4.5f;
+    const float R = rho - h;
+    const float base = 1.0f - 1.5f * u2;
+    // g collision (collisionPhase, src/lbm.cu:290-329):
+    //   geq_l = W_l [phi (1 + 3 c.u) + sharp_c phi (1 - phi) c.n]
+    // tau_g = 1 takes g* = geq as the reference does; otherwise BGK with omega_g.
+    const float A = sharp_c * phi * (1.0f - phi);
+    const float phi3 = 3.0f * phi;
+
+    float fo[kQ];
+    float go[kQ];
+    fo[0] = wf(0) * (base * R - om * tr3);
+    static_for<0, 9>([&](auto KC) {
+      constexpr int L = 2 * decltype(KC)::value + 1;
+      constexpr int O = L + 1;
+      constexpr float W = wf(L);
+      float cu = 0.f, cF = 0.f, cn = 0.f, qp = -tr3;
+      if constexpr (cx(L) != 0) { cu += cx(L) * ux; cF += cx(L) * Fx; cn += cx(L) * nc.x; qp += pxx; }
+      if constexpr (cy(L) != 0) { cu += cy(L) * uy; cF += cy(L) * Fy; cn += cy(L) * nc.y; qp += pyy; }
+      if constexpr (cz(L) != 0) { cu += cz(L) * uz; cF += cz(L) * Fz; cn += cz(L) * nc.z; qp += pzz; }
+      if constexpr (cx(L) * cy(L) != 0) qp += (2 * cx(L) * cy(L)) * pxy;
+      if constexpr (cx(L) * cz(L) != 0) qp += (2 * cx(L) * cz(L)) * pxz;
+      if constexpr (cy(L) * cz(L) != 0) qp += (2 * cy(L) * cz(L)) * pyz;
+      const float q = om * qp;
+      const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
+      const float rf = 1.5f * cF;
+      fo[L] = W * ((e0 + e1) * (R + rf) + q);
+      fo[O] = W * ((e0 - e1) * (R - rf) + q);
+      const float dg = phi3 * cu + A * cn;
+      go[L] = W * (phi + dg);
+      go[O] = W * (phi - dg);
+    });
+
+    static_for<0, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      fout[L * n + idx] = S::template f_enc<L>(fo[L]);
+    });
+
+    if constexpr (BGK) {
+      // Incoming g (pull), decoded, then relaxed towards geq.
+      const int pself = S::kDev ? __ldg(pprev + idx) : 0;
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr int O = opp(L);
+        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+        int gi;
+        if (bounce) {
+          gi = S::template g_dec<O>(S::gload(gin + (O - 1) * n + idx), pself);
+        } else {
+          const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                        src_of<cx(L)>(xm, x, xp);
+          const int ps = S::kDev ? __ldg(pprev + s) : 0;
+          gi = S::template g_dec<L>(S::gload(gin + (L - 1) * n + s), ps);
+        }
+        const float gf = __int2float_rn(gi) * kInvQ30;
+        go[L] = gf + omega_g * (go[L] - gf);
+      });
+    } else {
+      (void)omega_g;
+      (void)gin;
+      (void)rest_in;
+    }
+    int sumq = 0;
+    static_for<1, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      int q;
+      gout[(L - 1) * n + idx] = S::template g_enc<L>(go[L], pc, q);
+      sumq += q;
+    });
+    rest_out[idx] = S::rest_store(pc, sumq);
+
+    if (a.macros) {
+      const long long T = a.cells_total, o = t.cell_off + idx;
+      a.macros[o] = phi;
+      a.macros[T + o] = rho;
+      a.macros[2 * T + o] = ux;
+      a.macros[3 * T + o] = uy;
+      a.macros[4 * T + o] = uz;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ k_init: fields --
+
+// Writes the stored populations so that the first update gathers the equilibria of the
+// given fields: f_l(x) = feq_l(rho = 1, u(x)), g_l(x) = W_l phi(x) (1 + 3 c_l.u(x)).
+// In pull layout the value stored at y for direction l is the one its consumer y + c_l
+// reads; with bounce-back the consumer is y itself, as direction opp(l).
+// (initDist, src/init.cu:51-80.)
+template <class S>
+__global__ void k_init(const InitArgs a) {
+  using FT = typename S::FT;
+  using GT = typename S::GT;
+  const CaseDesc* cd = a.cases + a.case_index;
+  const int nx = cd->nx, ny = cd->ny, nz = cd->nz, bc = cd->bc;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= nx || y >= ny || z >= nz) return;
+  const long long n = cd->ncell, co = cd->cell_off;
+  const int idx = x + nx * (y + ny * z);
+  const bool ref = bc == kBcRef, walls = bc == kBcWallsZ;
+  const bool shell = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 ||
+                             z == nz - 1);
+  const float phi_self = a.phi[idx];
+  const int P = __float2int_rn(phi_self * kQ30);
+  a.p0[co + idx] = P;
+  a.p1[co + idx] = P;
+  const float ux_s = a.ux ? a.ux[idx] : 0.f;
+  const float uy_s = a.uy ? a.uy[idx] : 0.f;
+  const float uz_s = a.uz ? a.uz[idx] : 0.f;
+  if (a.macros) {
+    const long long T = a.cells_total;
+    a.macros[co + idx] = phi_self;
+    a.macros[T + co + idx] = 1.0f;
+    a.macros[2 * T + co + idx] = ux_s;
+    a.macros[3 * T + co + idx] = uy_s;
+    a.macros[4 * T + co + idx] = uz_s;
+  }
+  FT* f0 = static_cast<FT*>(a.f0) + cd->f_off;
+  FT* f1 = static_cast<FT*>(a.f1) + cd->f_off;
+  GT* g0 = static_cast<GT*>(a.g0) + cd->g_off;
+  static_for<0, kQ>([&](auto LC) {
+    constexpr int L = decltype(LC)::value;
+    int xc = x + cx(L), yc = y + cy(L), zc = z + cz(L);
+    bool bounce = false;
+    if (ref) {
+      if (xc < 0 || xc >= nx || yc < 0 || yc >= ny || zc < 0 || zc >= nz) {
+        xc = x;
+        yc = y;
+        zc = z;
+      }
+    } else {
+      xc = wrap1(xc, nx);
+      yc = wrap1(yc, ny);
+      if (walls && (zc < 0 || zc >= nz)) {
+        bounce = true;
+        zc = z;
+      } else {
+        zc = wrap1(zc, nz);
+      }
+    }
+    const int ci = xc + nx * (yc + ny * zc);
+    const float ux = a.ux ? a.ux[ci] : 0.f;
+    const float uy = a.uy ? a.uy[ci] : 0.f;
+    const float uz = a.uz ? a.uz[ci] : 0.f;
+    // Direction as seen by the consumer: opp(L) after a bounce.
+    const float sx = bounce ? -cx(L) : cx(L), sy = bounce ? -cy(L) : cy(L);
+    const float sz = bounce ? -cz(L) : cz(L);
+    const float cu = sx * ux + sy * uy + sz * uz;
+    const float u2 = ux * ux + uy * uy + uz * uz;
+    float feq = wf(L) * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
+    if (shell) feq = wf(L);
+    f0[L * n + idx] = S::template f_enc<L>(feq);
+    f1[L * n + idx] = S::template f_enc<L>(feq);
+    if constexpr (L == 0) {
+      a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
+    } else {
+      const float geq = wf(L) * a.phi[ci] * (1.0f + 3.0f * cu);
+      int q;
+      g0[(L - 1) * n + idx] = S::template g_enc<L>(geq, P, q);
+    }
+  });
+}
+
+// ------------------------------------------------------------------------ dispatch --
+
+template <class S>
+cudaError_t phi_variant(int variant, const StepArgs& a, cudaStream_t s) {
+  switch (variant) {
+    case 0: k_phi<S, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
+    case 1: k_phi<S, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
+    case 2: k_phi<S, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
+    case 3: k_phi<S, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <class S, bool BGK>
+cudaError_t collide_variant(int variant, const StepArgs& a, cudaStream_t s) {
+  switch (variant) {
+    case 0: k_collide<S, BGK, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
+    case 1: k_collide<S, BGK, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
+    case 2: k_collide<S, BGK, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
+    case 3: k_collide<S, BGK, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s) {
+  const dim3 block(32, 8);
+  const dim3 grid((nx + 31) / 32, (ny + 7) / 8, nz);
+  k_init<S><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// One storage format per translation unit, so the formats compile in parallel.
+#define MCB_STORAGE_LAUNCHERS(S, suffix)                                                   \
+  cudaError_t launch_phi_##suffix(int variant, const StepArgs& a, cudaStream_t s) {        \
+    return phi_variant<S>(variant, a, s);                                                  \
+  }                                                                                        \
+  cudaError_t launch_collide_##suffix(int variant, bool bgk, const StepArgs& a,            \
+                                      cudaStream_t s) {                                    \
+    return bgk ? collide_variant<S, true>(variant, a, s)                                   \
+               : collide_variant<S, false>(variant, a, s);                                 \
+  }                                                                                        \
+  cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
+                                   cudaStream_t s) {                                       \
+    return init_storage<S>(a, nx, ny, nz, s);                                              \
+  }
+
+}  // namespace
+}  // namespace mcb

@@ -1,0 +1,98 @@
+// Device-side case table and kernel arguments shared by the kernels and the host API.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcb {
+
+enum Bc : int { kBcRef = 0, kBcPeriodic = 1, kBcWallsZ = 2 };
+enum Storage : int { kStF32 = 0, kStF16 = 1, kStBF16 = 2 };
+
+// One case of a launch. A single-case handle has one entry. A batch has one entry per case,
+// and every case keeps its own offsets into the shared population buffers.
+struct CaseDesc {
+  int nx, ny, nz, bc;
+  int tiles_x, tiles_y, tiles_z, zchunk;  // tile decomposition of this launch
+  int tile0;                              // first tile (block) index of this case
+  int pad0;
+  long long ncell;     // nx*ny*nz
+  long long cell_off;  // offset of the case's cells in per-cell arrays (phi, rest, macros)
+  long long f_off;     // element offset of the case's 19*ncell f values
+  long long g_off;     // element offset of the case's 18*ncell moving g values
+  float omega;         // 1/tau
+  float omega_g;       // 1/tau_g
+  float sigma;
+  float sharp_c;
+  float gravity;
+  float phi_mean;      // mean phi of the initial field (buoyancy reference)
+};
+
+// Buffers of one update. Populations are stored post-collision at the cell that
+// collided them ("pull" layout): an update gathers f*(x - c_l, l).
+struct StepArgs {
+  const CaseDesc* cases;
+  int ncases;
+  int ntiles;
+  const void* f_in;   // 19 arrays per case
+  void* f_out;
+  const void* g_in;   // 18 moving g arrays per case (l = 1..18)
+  void* g_out;
+  const int* rest_in;  // g rest population, Q2.30 (per cell)
+  int* rest_out;
+  const int* p_prev;   // phi of the previous update, Q2.30
+  int* p_cur;          // phi of this update, Q2.30
+  float* macros;       // nullptr, or [5][cells_total]: phi, rho, ux, uy, uz
+  long long cells_total;
+  int first;           // 1 on the first update after fields were set
+};
+
+struct InitArgs {
+  const CaseDesc* cases;
+  int case_index;
+  const float* phi;   // host-provided initial fields of this case (device copies)
+  const float* ux;    // may be nullptr (rest)
+  const float* uy;
+  const float* uz;
+  void* f0;
+  void* f1;
+  void* g0;
+  int* rest0;
+  int* p0;
+  int* p1;
+  float* macros;
+  long long cells_total;
+};
+
+// Per-block partial sums of the diagnostics reduction.
+struct DiagPartial {
+  double mass, ke, umax, rho_in, n_in, rho_out, n_out, vol_half, phi_min, phi_max;
+  long long mass_q30;
+  long long nonfinite;
+};
+
+struct DiagArgs {
+  const CaseDesc* cases;
+  int case_index;
+  const float* macros;
+  const int* p;        // latest phi, Q2.30
+  long long cells_total;
+  DiagPartial* partials;  // gridDim.x entries
+  DiagPartial* result;    // one entry
+};
+
+constexpr int kNumVariants = 4;
+struct Variant { int bx, by; };
+constexpr Variant kVariants[kNumVariants] = {{32, 8}, {16, 16}, {64, 4}, {16, 8}};
+constexpr int kDiagBlocks = 304;   // fixed grid: the reduction order never changes
+constexpr int kDiagThreads = 256;
+
+// Kernel launchers (kernels.cu). Each returns the launch status.
+cudaError_t launch_phi(int storage, int variant, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_collide(int storage, int variant, bool bgk, const StepArgs& a,
+                           cudaStream_t s);
+cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
+                        cudaStream_t s);
+cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s);
+
+}  // namespace mcb

@@ -1,0 +1,260 @@
+"""Parity of the CUDA solver (through the C ABI) with the FP64 CPU oracle and with the
+reference's own kernels, plus its exact invariants. All of these need the GB300."""
+import numpy as np
+import pytest
+
+import mcb
+from oracle.oracle import Oracle, ReferenceKernels, harness_available
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("phi", "rho", "ux", "uy", "uz")
+
+
+def gpu_run(cfg, phi, u=None, steps=10, **over):
+    for k, v in over.items():
+        setattr(cfg, k, v)
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, *(u if u is not None else (None, None, None)))
+        s.step(steps)
+        out = {k: s.get(k).astype(np.float64) for k in FIELDS}
+        out["diag"] = s.diagnostics()
+    return out
+
+
+def oracle_run(cfg, phi, u=None, steps=10, precision=64):
+    o = Oracle.from_config(cfg, precision=precision)
+    o.set_fields(phi, *(u if u is not None else (None, None, None)))
+    o.step(steps)
+    out = {k: o.get(k) for k in FIELDS}
+    out["diag"] = o.diagnostics()
+    return out
+
+
+def maxdiff(a, b, k):
+    return float(np.max(np.abs(a[k] - b[k])))
+
+
+def small_case(bc, n=(24, 20, 28), tau_g=1.0, gravity=0.0, noise=0.0, seed=0):
+    nx, ny, nz = n
+    cfg = mcb.default_config(nx=nx, ny=ny, nz=nz, bc=bc, tau=0.7, tau_g=tau_g, sigma=0.05,
+                             width=4.0, sharp_c=0.0, gravity=gravity)
+    phi = mcb.fill_phi_bubbles(nx, ny, nz, bc, 4.0, [(nx * 0.45, ny * 0.5, nz * 0.4, 5.0),
+                                                     (nx * 0.8, ny * 0.2, nz * 0.8, 3.0)])
+    u = None
+    if noise:
+        rng = np.random.default_rng(seed)
+        u = tuple((noise * rng.standard_normal(phi.shape)).astype(np.float32) for _ in range(3))
+    return cfg, phi, u
+
+
+# Max |GPU FP32 - FP64 oracle| after 30 updates on the small cases. The float32 rounding
+# of one update is ~1e-7 relative; 30 updates of this dissipative system stay well below
+# these bounds.
+TOL = {"phi": 2e-5, "rho": 2e-5, "ux": 2e-6, "uy": 2e-6, "uz": 2e-6}
+
+
+@pytest.mark.parametrize("bc,tau_g,gravity,noise", [
+    (mcb.BC_PERIODIC, 1.0, 0.0, 0.0),
+    (mcb.BC_PERIODIC, 0.8, 0.0, 1e-3),
+    (mcb.BC_WALLS_Z, 1.0, 1e-4, 0.0),
+    (mcb.BC_WALLS_Z, 0.8, 1e-4, 1e-3),
+])
+def test_f32_matches_fp64_oracle(bc, tau_g, gravity, noise):
+    cfg, phi, u = small_case(bc, tau_g=tau_g, gravity=gravity, noise=noise)
+    g = gpu_run(cfg, phi, u, steps=30)
+    o = oracle_run(cfg, phi, u, steps=30)
+    for k, tol in TOL.items():
+        assert maxdiff(g, o, k) < tol, (k, maxdiff(g, o, k))
+
+
+def off_centre_reference_phi(n, r=8.0):
+    """Reference-mode bubble whose centre is not a lattice node (shell left at 0)."""
+    return mcb.fill_phi_bubbles(n, n, n, mcb.BC_REF, 4.0,
+                                [(n / 2 - 0.3, n / 2 + 0.35, n / 2 + 0.45, r)])
+
+
+def reference_cfg(n):
+    cfg, *_ = mcb.workload(0, scale=n / 64, fields=False)  # tau 0.8, sigma 0.1, W 4
+    assert (cfg.nx, cfg.bc, cfg.tau_g) == (n, mcb.BC_REF, 1.0)
+    return cfg
+
+
+def test_reference_mode_matches_fp64_oracle():
+    n = 32
+    cfg = reference_cfg(n)
+    phi = off_centre_reference_phi(n)
+    g = gpu_run(cfg, phi, steps=100)
+    o = oracle_run(cfg, phi, steps=100)
+    for k, tol in TOL.items():
+        assert maxdiff(g, o, k) < tol, (k, maxdiff(g, o, k))
+    # the shell of phi holds the zero-gradient copy, as in the reference's dumps
+    assert np.array_equal(g["phi"][0, 1:-1, 1:-1], g["phi"][1, 1:-1, 1:-1])
+
+
+def test_reference_init_short_horizon_matches_fp64_oracle():
+    """The reference's own node-centred bubble (src/init.cu:27-49). Its centre node makes
+    the run sensitive to rounding after a few updates, so the horizon is short."""
+    n = 32
+    cfg = reference_cfg(n)
+    phi = mcb.fill_phi_reference(n, n, n, 8.0, 4.0)
+    g = gpu_run(cfg, phi, steps=4)
+    o = oracle_run(cfg, phi, steps=4)
+    for k in FIELDS:
+        assert maxdiff(g, o, k) < 2e-6, (k, maxdiff(g, o, k))
+
+
+def _reference_kernels(cfg, phi, steps):
+    n = cfg.nx
+    sharp = (cfg.tau_g - 0.5) * 4.0 / cfg.width
+    rk = ReferenceKernels(n, n, n, cfg.tau, cfg.sigma, sharp)
+    rk.set_phi(phi)
+    rk.run(steps)
+    out = {k: rk.get(k).astype(np.float64) for k in FIELDS}
+    rk.close()
+    return out
+
+
+@pytest.mark.skipif(not harness_available(), reason="reference cubin not built")
+@pytest.mark.parametrize("init,steps,tol", [("off_centre", 300, TOL),
+                                            ("reference", 4, {k: 2e-6 for k in FIELDS})])
+def test_reference_mode_matches_reference_kernels(init, steps, tol):
+    """The reference's own kernels (unmodified src/lbm.cu for sm_103a) and the fused solver,
+    from the same initial phi, 32^3. The comparison excludes the shell, whose edges the
+    reference writes racily (src/lbm.cu:411-424)."""
+    n = 32
+    cfg = reference_cfg(n)
+    phi = off_centre_reference_phi(n) if init == "off_centre" else \
+        mcb.fill_phi_reference(n, n, n, 8.0, 4.0)
+    ref = _reference_kernels(cfg, phi, steps)
+    g = gpu_run(cfg, phi, steps=steps)
+    inner = (slice(1, -1),) * 3
+    for k in FIELDS:
+        d = float(np.max(np.abs(g[k][inner] - ref[k][inner])))
+        assert d < tol[k], (k, d)
+
+
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
+@pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z])
+def test_phi_mass_is_exactly_conserved(storage, bc):
+    cfg, phi, u = small_case(bc, tau_g=0.8 if bc == mcb.BC_PERIODIC else 1.0,
+                             gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, *u)
+        s.step(1)
+        m0 = s.diagnostics()["mass_q30"]
+        for _ in range(5):
+            s.step(37)
+            assert s.diagnostics()["mass_q30"] == m0
+
+
+@pytest.mark.parametrize("storage,tol", [(mcb.STORE_F16, 1e-3), (mcb.STORE_BF16, 1e-3)])
+def test_16bit_storage_stays_close_to_fp64(storage, tol):
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(32, 32, 32), noise=1e-4)
+    o = oracle_run(cfg, phi, u, steps=200)
+    g = gpu_run(cfg, phi, u, steps=200, storage=storage)
+    assert maxdiff(g, o, "phi") < tol
+    assert maxdiff(g, o, "ux") < 1e-4
+
+
+def test_tile_variants_graphs_and_chunks_agree_bitwise():
+    cfg, phi, u = small_case(mcb.BC_WALLS_Z, n=(40, 36, 30), tau_g=0.8, gravity=1e-4,
+                             noise=1e-3)
+    base = gpu_run(cfg, phi, u, steps=41, variant=0, use_graph=0, zchunk=0)
+    for v in range(mcb.lib().mcb_variant_count()):
+        for g in (0, 1):
+            for zc in (0, 4, 7):
+                r = gpu_run(cfg, phi, u, steps=41, variant=v, use_graph=g, zchunk=zc)
+                for k in FIELDS:
+                    assert np.array_equal(r[k], base[k]), (v, g, zc, k)
+
+
+def test_steps_split_across_calls_agree_bitwise():
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, tau_g=0.8, noise=1e-3)
+    one = gpu_run(cfg, phi, u, steps=50)
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, *u)
+        for n in (1, 17, 3, 29):
+            s.step(n)
+        assert s.update == 49
+        for k in FIELDS:
+            assert np.array_equal(s.get(k).astype(np.float64), one[k]), k
+
+
+def test_batch_matches_single_cases_bitwise():
+    cases = []
+    for i, (n, bc, storage) in enumerate([((16, 16, 16), mcb.BC_PERIODIC, mcb.STORE_F16),
+                                          ((24, 20, 28), mcb.BC_WALLS_Z, mcb.STORE_F16),
+                                          ((32, 32, 32), mcb.BC_PERIODIC, mcb.STORE_F16)]):
+        cfg, phi, u = small_case(bc, n=n, noise=1e-3, seed=i, gravity=1e-4 * (i == 1))
+        cfg.storage = storage
+        cfg.tau = 0.6 + 0.1 * i
+        cases.append((cfg, phi, u))
+    with mcb.Batch([c for c, _, _ in cases]) as b:
+        for i, (c, phi, u) in enumerate(cases):
+            b.set_fields(i, phi, *u)
+        b.step(33)
+        got = [{k: b.get(i, k) for k in FIELDS} for i in range(len(cases))]
+        dg = [b.diagnostics(i) for i in range(len(cases))]
+    for i, (c, phi, u) in enumerate(cases):
+        single = gpu_run(c, phi, u, steps=33)
+        for k in FIELDS:
+            assert np.array_equal(got[i][k].astype(np.float64), single[k]), (i, k)
+        assert dg[i]["mass_q30"] == single["diag"]["mass_q30"]
+
+
+def test_rest_state_is_a_fixed_point():
+    n = 16
+    cfg = mcb.default_config(nx=n, ny=n, nz=n, bc=mcb.BC_PERIODIC, tau=0.7, tau_g=1.0,
+                             width=4.0, sharp_c=0.0)
+    for storage in (mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16):
+        g = gpu_run(cfg, np.full((n, n, n), 0.25, np.float32), steps=20, storage=storage)
+        assert np.max(np.abs(g["phi"] - 0.25)) < 1e-6
+        assert np.max(np.abs(g["rho"] - 1.0)) < 1e-6
+        assert np.max(np.abs(g["ux"])) < 1e-7
+
+
+def test_dump_files_hold_the_phi_field(tmp_path):
+    cfg, phi, u = small_case(mcb.BC_PERIODIC)
+    d = str(tmp_path) + "/"
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi)
+        s.step(5)
+        s.dump_phi(d, "001", 4)
+        s.write_info(d, "001", nsteps=4)
+        want = s.get("phi")
+    raw = np.fromfile(tmp_path / "001_phi000004.bin", np.float32)
+    assert np.array_equal(raw.reshape(want.shape), want)
+    text = (tmp_path / "001_info.txt").read_text()
+    assert "Precision: float" in text and "NZ_TOTAL: 28" in text
+
+
+def test_autotune_restores_the_state():
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(32, 32, 32), noise=1e-3)
+    ref = gpu_run(cfg, phi, u, steps=20)
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, *u)
+        s.step(10)
+        v, zc, ml = s.autotune(nsteps=4)
+        assert 0 <= v < mcb.lib().mcb_variant_count() and zc > 0 and ml > 0
+        s.step(10)
+        for k in FIELDS:
+            assert np.array_equal(s.get(k).astype(np.float64), ref[k]), k
+
+
+def test_errors_come_back_as_status_codes():
+    cfg, phi, _ = small_case(mcb.BC_PERIODIC)
+    with mcb.Solver(cfg) as s:
+        with pytest.raises(mcb.McbError) as e:
+            s.step(1)  # fields not set
+        assert e.value.code == mcb.ERR_STATE
+        s.set_fields(phi)
+        with pytest.raises(mcb.McbError) as e:
+            s.get(17)
+        assert e.value.code == mcb.ERR_INVALID
+        bad = phi.copy()
+        bad[3, 3, 3] = np.nan
+        with pytest.raises(mcb.McbError) as e:
+            s.set_fields(bad)
+        assert e.value.code == mcb.ERR_INVALID

@@ -1,0 +1,164 @@
+"""The CPU oracle on its own: known answers of the restated reference update.
+
+The reference has no tests, fixtures or golden vectors. These checks are the physics
+known-answers, plus the algebra the fused kernel relies on.
+"""
+import numpy as np
+import pytest
+
+import mcb
+from oracle.oracle import Oracle
+
+CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
+CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1])
+CZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1])
+W = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+C = np.stack([CX, CY, CZ], 1).astype(np.float64)
+
+
+def test_d3q19_isotropy_used_by_the_closed_form_moments():
+    """The fused kernel replaces the per-population sums of momentiCalc (src/lbm.cu:201-218)
+    by closed forms. Those hold because D3Q19 is isotropic to 4th order."""
+    rng = np.random.default_rng(3)
+    cs2 = 1 / 3
+    assert np.isclose(W.sum(), 1)
+    assert np.allclose(np.einsum("l,la,lb->ab", W, C, C), cs2 * np.eye(3))
+    for _ in range(20):
+        rho = 1 + 0.05 * rng.standard_normal()
+        u = 0.05 * rng.standard_normal(3)
+        F = 1e-3 * rng.standard_normal(3)
+        cu = C @ u
+        E = 1 + 3 * cu + 4.5 * cu**2 - 1.5 * u @ u
+        feq = W * rho * E
+        hef = 0.5 * feq * ((C - u) @ F) * 3 / rho
+        m_eq = np.einsum("l,la,lb->ab", feq, C, C)
+        m_he = np.einsum("l,la,lb->ab", hef, C, C)
+        assert np.allclose(m_eq, rho * (cs2 * np.eye(3) + np.outer(u, u)), atol=1e-14)
+        want = 0.5 * (np.outer(u, F) + np.outer(F, u)) - 1.5 * (u @ F) * np.outer(u, u)
+        assert np.allclose(m_he, want, atol=1e-15)
+        # regularised post-collision population in the kernel's pair form
+        Pi = rng.standard_normal((3, 3)) * 1e-3
+        Pi = Pi + Pi.T
+        om = 1 / 0.7
+        Q = np.einsum("la,lb->lab", C, C) - cs2 * np.eye(3)
+        ref = feq + (1 - om) * W / (2 * cs2**2) * np.einsum("lab,ab->l", Q, Pi) + hef
+        R = rho - 1.5 * (u @ F)
+        qp = np.einsum("lab,ab->l", Q, Pi)
+        mine = W * (E * (R + 1.5 * (C @ F)) + 4.5 * (1 - om) * qp)
+        assert np.allclose(mine, ref, atol=1e-15)
+
+
+def test_isotropic_gradient_is_exact_on_quadratics():
+    """gradCalc's stencil (src/lbm.cu:51-63): sum 3 W_l c_l phi(x + c_l) is exact for
+    polynomials of degree <= 2."""
+    rng = np.random.default_rng(1)
+    for _ in range(10):
+        a = rng.standard_normal(3)
+        B = rng.standard_normal((3, 3))
+        B = B + B.T
+        x0 = rng.standard_normal(3)
+        phi = lambda x: a @ x + 0.5 * x @ B @ x
+        grad = sum(3 * W[l] * C[l] * phi(x0 + C[l]) for l in range(19))
+        assert np.allclose(grad, a + B @ x0, atol=1e-12)
+
+
+def _bubble(n, bc=mcb.BC_PERIODIC, r=None, width=4.0):
+    return mcb.fill_phi_bubbles(n, n, n, bc, width, [(n / 2, n / 2, n / 2, r or n / 5)])
+
+
+@pytest.mark.parametrize("phi0", [0.0, 0.3, 1.0])
+def test_uniform_rest_state_stays_fixed(built, phi0):
+    n = 12
+    o = Oracle(n, n, n, mcb.BC_PERIODIC, 0.7, 1.0, 0.1, 0.5)
+    o.set_fields(np.full((n, n, n), phi0, np.float32))
+    o.step(20)
+    assert np.max(np.abs(o.get("phi") - float(np.float32(phi0)))) < 1e-13
+    assert np.max(np.abs(o.get("rho") - 1.0)) < 1e-13
+    for k in ("ux", "uy", "uz"):
+        assert np.max(np.abs(o.get(k))) < 1e-15
+
+
+@pytest.mark.parametrize("bc,gravity,tau_g", [(mcb.BC_PERIODIC, 0.0, 1.0),
+                                              (mcb.BC_PERIODIC, 0.0, 0.8),
+                                              (mcb.BC_WALLS_Z, 1e-4, 1.0)])
+def test_phi_mass_is_conserved_in_closed_domains(built, bc, gravity, tau_g):
+    n = 16
+    phi = mcb.fill_phi_bubbles(n, n, n, bc, 4.0, [(8, 8, 6, 4), (4, 3, 12, 2.5)])
+    o = Oracle(n, n, n, bc, 0.7, tau_g, 0.05, (tau_g - 0.5), gravity)
+    o.set_fields(phi)
+    o.step(1)
+    m0 = o.diagnostics()["mass"]
+    o.step(60)
+    m1 = o.diagnostics()["mass"]
+    assert abs(m1 - m0) / m0 < 1e-12
+
+
+def test_centred_bubble_keeps_mirror_symmetry(built):
+    """Symmetric in exact arithmetic. Round-off breaks it, and the sharpening flux
+    sharp_c phi (1 - phi) n amplifies that wherever |grad phi| is tiny next to phi (1 - phi):
+    in the tanh tails and between periodic images. So the check uses a short horizon."""
+    n = 24
+    phi = _bubble(n, r=6)
+    o = Oracle(n, n, n, mcb.BC_PERIODIC, 0.8, 1.0, 0.1, 0.5)
+    o.set_fields(phi)
+    o.step(6)
+    p = o.get("phi")
+    ux = o.get("ux")
+    # cell i mirrors cell (n - i) mod n about the centre n/2
+    idx = (-np.arange(n)) % n
+    assert np.max(np.abs(p - p[:, :, idx])) < 1e-12
+    assert np.max(np.abs(p - p.transpose(0, 2, 1))) < 1e-12
+    assert np.max(np.abs(ux + ux[:, :, idx])) < 1e-13
+
+
+def test_moving_wall_writes_have_no_effect(built):
+    """movingWallBC (src/lbm.cu:430-461) writes f only on shell cells, which nothing reads:
+    the solver leaves it out."""
+    n = 16
+    phi = mcb.fill_phi_reference(n, n, n, 4.0, 4.0)
+    runs = []
+    for mw in (True, False):
+        o = Oracle(n, n, n, mcb.BC_REF, 0.8, 1.0, 0.1, 0.5, moving_wall=mw)
+        o.set_fields(phi)
+        o.step(25)
+        runs.append({k: o.get(k) for k in ("phi", "rho", "ux", "uy", "uz")})
+    for k in runs[0]:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+def off_centre_reference_phi(n, r=8.0):
+    """A reference-mode bubble whose centre is not a lattice node (shell left at 0)."""
+    return mcb.fill_phi_bubbles(n, n, n, mcb.BC_REF, 4.0,
+                                [(n / 2 - 0.3, n / 2 + 0.35, n / 2 + 0.45, r)])
+
+
+def test_fp32_restatement_tracks_fp64(built):
+    """Off-centre bubble: the float restatement stays within float noise of FP64."""
+    n = 32
+    res = []
+    for prec in (64, 32):
+        o = Oracle(n, n, n, mcb.BC_REF, 0.8, 1.0, 0.1, 0.5, precision=prec)
+        o.set_fields(off_centre_reference_phi(n))
+        o.step(100)
+        res.append({k: o.get(k) for k in ("phi", "ux", "rho")})
+    assert np.max(np.abs(res[0]["phi"] - res[1]["phi"])) < 5e-5
+    assert np.max(np.abs(res[0]["rho"] - res[1]["rho"])) < 1e-5
+    assert np.max(np.abs(res[0]["ux"] - res[1]["ux"])) < 2e-6
+
+
+def test_node_centred_bubble_amplifies_rounding(built):
+    """The reference's init (src/init.cu:27-49) centres the bubble on a lattice node.
+    There grad phi = 0, and the normal grad phi * rsqrt(max(|grad phi|^2, 1e-9))
+    (src/lbm.cu:65-70) scales the rounding noise of grad phi by up to 3e4. Float and double
+    therefore part by ~1e-3 at that node within 10 updates. They agree to rounding for
+    the first few updates."""
+    n = 32
+    phi = mcb.fill_phi_reference(n, n, n, 8.0, 4.0)
+    runs = [Oracle(n, n, n, mcb.BC_REF, 0.8, 1.0, 0.1, 0.5, precision=p) for p in (64, 32)]
+    for o in runs:
+        o.set_fields(phi)
+        o.step(4)
+    assert np.max(np.abs(runs[0].get("phi") - runs[1].get("phi"))) < 2e-6
+    for o in runs:
+        o.step(6)
+    assert np.max(np.abs(runs[0].get("phi") - runs[1].get("phi"))) > 1e-4
