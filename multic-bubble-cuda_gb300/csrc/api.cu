@@ -54,6 +54,8 @@ int validate(const mcb_config& c, int index) {
   if (c.nx < 4 || c.ny < 4 || c.nz < 4)
     return fail(MCB_ERR_INVALID, "case %d: lattice %dx%dx%d is below 4 cells per axis", index,
                 c.nx, c.ny, c.nz);
+  if (c.nx > 65535 || c.ny > 65535 || c.nz > 65535)
+    return fail(MCB_ERR_INVALID, "case %d: an axis exceeds 65535 cells", index);
   const long long n = static_cast<long long>(c.nx) * c.ny * c.nz;
   if (n > 0x7fffffffLL)
     return fail(MCB_ERR_INVALID, "case %d: %lld cells exceed 2^31-1 per case", index, n);
