@@ -135,10 +135,13 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
+SCALE = 1.0
+
+
 def make_solver(storage: str, device: int):
     import mcb
 
-    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED)
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=SCALE)
     cfg.storage = mcb.STORAGES[storage]
     cfg.device = device
     s = mcb.Solver(cfg)
@@ -295,7 +298,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="solver", choices=["solver", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="length scale of the workload (profiling runs use a smaller case)")
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"],
+                    help="population storage of the device leg (the headline is f32)")
+    ap.add_argument("--only-device", action="store_true",
+                    help="time the device loop only (no fp16, e2e, reference or CPU legs)")
     args = ap.parse_args()
+    global SCALE
+    SCALE = args.scale
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, ws, rank)
@@ -315,41 +326,47 @@ def main():
     dev = torch.device("cuda", local)
 
     with Clocks(local) as clk:
-        cfg, total_ms, phi_ms, col_ms, diag = device_run("f32", local, args.steps, args.warmup,
-                                                         dist)
+        cfg, total_ms, phi_ms, col_ms, diag = device_run(args.storage, local, args.steps,
+                                                         args.warmup, dist)
     t_max = reduce_max(dist, total_ms, dev)
     cells = cfg.nx * cfg.ny * cfg.nz
     value = ws * cells * args.steps / (t_max * 1e-3) / 1e6
     hbm, peak_kind = peaks()
     col_avg_s = col_ms * 1e-3 / args.steps
-    achieved = COLLIDE_BYTES_PER_LU["f32"] * cells / col_avg_s / 1e9
-    update_achieved = BYTES_PER_LU["f32"] * cells / (total_ms * 1e-3 / args.steps) / 1e9
+    st = args.storage
+    achieved = COLLIDE_BYTES_PER_LU[st] * cells / col_avg_s / 1e9
+    update_achieved = BYTES_PER_LU[st] * cells / (total_ms * 1e-3 / args.steps) / 1e9
     result = {
         "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "rising perturbed bubble 128x128x256, walls z, gravity 1e-5, "
-                               "Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 storage",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "storage": st,
+        "data": "synthetic",
+        "config": {"workload": f"rising perturbed bubble {cfg.nx}x{cfg.ny}x{cfg.nz}, walls z, "
+                               "gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 "
+                               "storage",
                    "cells": cells, "l2": "inputs larger than L2 (f+g 637 MB per update)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
         "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": f"{peak_kind} HBM copy bandwidth",
-                     "bytes_per_lu": COLLIDE_BYTES_PER_LU["f32"],
+                     "bytes_per_lu": COLLIDE_BYTES_PER_LU[st],
                      "traffic": traffic_per_launch(cells),
                      "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
-                     "update_bytes_per_lu": BYTES_PER_LU["f32"],
+                     "update_bytes_per_lu": BYTES_PER_LU[st],
                      "kernel_ms": {"k_phi": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
         "mass_q30_finite": bool(diag["finite"]),
     }
-    if rank == 0:
+    if rank == 0 and args.only_device:
+        print(json.dumps(result))
+    elif rank == 0:
         _, t16, p16, c16, d16 = device_run("f16", local, args.steps, args.warmup, None)
         v16 = cells * args.steps / (t16 * 1e-3) / 1e6
         result["fp16"] = {"value": v16, "unit": "MLUPS", "ratio_vs_f32": v16 / (value / ws),
                           "frac_update": BYTES_PER_LU["f16"] * cells / (t16 * 1e-3 / args.steps)
-                          / 1e9 / hbm}
+                          / 1e9 / hbm,
+                          "kernel_ms": {"k_phi": p16 / args.steps, "k_collide": c16 / args.steps}}
         result["e2e"] = e2e_run(local, args.steps)
         result["reference_cuda"] = reference_cuda_run(local, min(args.steps, 200))
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
