@@ -158,6 +158,30 @@ __device__ __forceinline__ int wrap1(int v, int n) {
 }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
+__device__ __forceinline__ void l2_prefetch(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// L2 prefetch of one plane of a BX x BY tile in narr arrays: the first and the last
+// element of every row, which covers each row's one or two 128-byte lines. A later update
+// loop iteration then finds these populations in L2. That keeps DRAM busy regardless of
+// how many warps are resident. Every address lies inside the arrays.
+template <int NT, int BX, int BY>
+__device__ __forceinline__ void prefetch_rows(int tid, const char* base, long long arr_bytes,
+                                              int narr, int elem, long long plane_elems,
+                                              int xt, int yt, int nx, int ny) {
+  const int x_last = min(xt + BX, nx) - 1;
+  const int total = narr * BY * 2;
+  for (int j = tid; j < total; j += NT) {
+    const int side = j & 1, r = (j >> 1) % BY, arr = (j >> 1) / BY;
+    const int y = yt + r;
+    if (y >= ny) continue;
+    const int x = side ? x_last : xt;
+    l2_prefetch(base + arr * arr_bytes +
+                (plane_elems + static_cast<long long>(y) * nx + x) * elem);
+  }
+}
+
 __device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int tile) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
@@ -218,8 +242,21 @@ __global__ void __launch_bounds__(BX * BY) k_phi(const StepArgs a) {
   const int ym = (y == 0 ? ny - 1 : y - 1) * nx, yo = y * nx;
   const int yp = (y == ny - 1 ? 0 : y + 1) * nx;
   const bool shell_xy = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1);
+  const int tid = threadIdx.x + BX * threadIdx.y;
+  auto prefetch = [&](int zpl) {
+    const long long po = static_cast<long long>(zpl) * nxy;
+    prefetch_rows<BX * BY, BX, BY>(tid, reinterpret_cast<const char*>(gin), n * sizeof(GT),
+                                   kQ - 1, sizeof(GT), po, t.xt, t.yt, nx, ny);
+    prefetch_rows<BX * BY, BX, BY>(tid, reinterpret_cast<const char*>(rest), 0, 1, 4, po,
+                                   t.xt, t.yt, nx, ny);
+    if (S::kDev)
+      prefetch_rows<BX * BY, BX, BY>(tid, reinterpret_cast<const char*>(pprev), 0, 1, 4, po,
+                                     t.xt, t.yt, nx, ny);
+  };
+  if (t.zb + 1 < nz) prefetch(t.zb + 1);
 
   for (int z = t.zb; z < t.ze; ++z) {
+    if (z + 2 < nz && z + 2 <= t.ze) prefetch(z + 2);
     const int zo = z * nxy;
     const int idx = x + yo + zo;
     int P;
@@ -268,7 +305,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
   constexpr int HX = BX + 2, HY = BY + 2, HP = HX * HY;  // normals plane, halo 1
   constexpr int KPF = (PP + NT - 1) / NT;                // phi values per thread per plane
   __shared__ float sphi[5][PP];
-  __shared__ float4 snrm[3][HP];
+  __shared__ float snrm[3][4][HP];  // nx, ny, nz, |grad phi| of three planes
 
   const Tile t = locate_tile<BX, BY>(a);
   const int nx = t.nx, ny = t.ny, nz = t.nz;
@@ -325,7 +362,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
     const float* pm = sphi[(zp + 4) % 5];
     const float* p0 = sphi[(zp + 5) % 5];
     const float* pp = sphi[(zp + 6) % 5];
-    float4* dst = snrm[(zp + 3) % 3];
+    float(*dst)[HP] = snrm[(zp + 3) % 3];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
     for (int i = tid; i < HP; i += NT) {
       const int hx = i % HX, hy = i / HX;
@@ -347,7 +384,10 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
         const float fac = rsqrtf(fmaxf(g2, 1e-9f));
         r = make_float4(gxs * fac, gys * fac, gzs * fac, g2 * fac);
       }
-      dst[i] = r;
+      dst[0][i] = r.x;
+      dst[1][i] = r.y;
+      dst[2][i] = r.z;
+      dst[3][i] = r.w;
     }
   };
 
@@ -366,6 +406,13 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
   int* __restrict__ rest_out = a.rest_out + t.cell_off;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
+  auto prefetch_f = [&](int zpl) {
+    prefetch_rows<NT, BX, BY>(tid, reinterpret_cast<const char*>(fin), n * sizeof(FT), kQ,
+                              sizeof(FT), static_cast<long long>(zpl) * nxy, t.xt, t.yt, nx,
+                              ny);
+  };
+  if (t.zb + 1 < nz) prefetch_f(t.zb + 1);
+
   // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
   for (int zpl = t.zb - 2; zpl <= t.zb + 1; ++zpl) {
     issue(zpl);
@@ -379,6 +426,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
   for (int z = t.zb; z < t.ze; ++z) {
     commit(z + 2);
     if (z + 3 <= t.ze + 1) issue(z + 3);
+    if (z + 2 < nz && z + 2 <= t.ze) prefetch_f(z + 2);
 
     const int zo = z * nxy;
     const int idx = x + yo + zo;
@@ -430,21 +478,23 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
       continue;
     }
 
-    // Curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125).
-    const float4* nm = snrm[(z + 2) % 3];
-    const float4* n0 = snrm[(z + 3) % 3];
-    const float4* np = snrm[(z + 4) % 3];
+    // Curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125). Each neighbour
+    // contributes c.n, so only the components along its nonzero c are read.
+    const float(*nm)[HP] = snrm[(z + 2) % 3];
+    const float(*n0)[HP] = snrm[(z + 3) % 3];
+    const float(*np)[HP] = snrm[(z + 4) % 3];
     const int hc = (ty + 1) * HX + tx + 1;
-    const float4 nc = n0[hc];
+    const float4 nc = make_float4(n0[0][hc], n0[1][hc], n0[2][hc], n0[3][hc]);
     float kap = 0.f;
     static_for<1, kQ>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
       constexpr float w3 = 3.0f * wf(L);
-      const float4 nb = nbr_of<cz(L)>(nm, n0, np)[hc + cy(L) * HX + cx(L)];
+      const float(*pl)[HP] = nbr_of<cz(L)>(nm, n0, np);
+      const int o = hc + cy(L) * HX + cx(L);
       float cn = 0.f;
-      if constexpr (cx(L) != 0) cn += cx(L) * nb.x;
-      if constexpr (cy(L) != 0) cn += cy(L) * nb.y;
-      if constexpr (cz(L) != 0) cn += cz(L) * nb.z;
+      if constexpr (cx(L) != 0) cn += cx(L) * pl[0][o];
+      if constexpr (cy(L) != 0) cn += cy(L) * pl[1][o];
+      if constexpr (cz(L) != 0) cn += cz(L) * pl[2][o];
       kap -= w3 * cn;
     });
     const float phi = sphi[(z + 5) % 5][(ty + 2) * PX + tx + 2];
@@ -634,7 +684,10 @@ __global__ void k_init(const InitArgs a) {
       xc = wrap1(xc, nx);
       yc = wrap1(yc, ny);
       if (walls && (zc < 0 || zc >= nz)) {
+        // Half-way bounce-back: the population returns to the cell it left.
         bounce = true;
+        xc = x;
+        yc = y;
         zc = z;
       } else {
         zc = wrap1(zc, nz);

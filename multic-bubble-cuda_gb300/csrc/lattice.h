@@ -42,15 +42,31 @@ MCB_HD constexpr double wd(int l) {
   return l == 0 ? (1.0 / 3.0) : (l <= 6 ? (1.0 / 18.0) : (1.0 / 36.0));
 }
 
-// Exact integer split of a Q2.30 phi value over the 19 weights: the moving parts are
-// P/18 and P/36 (C division), the rest part takes the remainder, so the 19 parts add
-// back to P exactly. Used for the weight part of the 16-bit deviation form.
-MCB_HD constexpr int wsplit_face(int p) { return p / 18; }
-MCB_HD constexpr int wsplit_edge(int p) { return p / 36; }
-MCB_HD constexpr int wsplit_rest(int p) { return p - 6 * (p / 18) - 12 * (p / 36); }
+// Exact integer split of a Q2.30 phi value over the 19 weights, for the weight part of the
+// 16-bit deviation form:
+//   - a face part ~ P/18: the high word of P * ceil(2^32/18), one multiply;
+//   - an edge part: half of the face part;
+//   - the rest part: the remainder.
+// So the 19 parts add back to P exactly. Any deterministic split would keep the phi sum
+// exact; this one keeps every part within one unit of W_l * P.
+MCB_HD int wsplit_face(int p) {
+#if defined(__CUDA_ARCH__)
+  return __mulhi(p, 238609295);
+#else
+  return static_cast<int>((static_cast<long long>(p) * 238609295LL) >> 32);
+#endif
+}
+MCB_HD int wsplit_edge_of_face(int wf) { return wf >> 1; }
+MCB_HD int wsplit_edge(int p) { return wsplit_edge_of_face(wsplit_face(p)); }
+MCB_HD int wsplit_rest(int p) {
+  const int f = wsplit_face(p);
+  return p - 6 * f - 12 * wsplit_edge_of_face(f);
+}
 template <int L>
-MCB_HD constexpr int wsplit(int p) {
-  return L == 0 ? wsplit_rest(p) : (L <= 6 ? wsplit_face(p) : wsplit_edge(p));
+MCB_HD int wsplit(int p) {
+  if constexpr (L == 0) return wsplit_rest(p);
+  else if constexpr (L <= 6) return wsplit_face(p);
+  else return wsplit_edge(p);
 }
 
 // Q2.30 fixed point: 1.0 = 2^30.

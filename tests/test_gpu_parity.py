@@ -57,6 +57,8 @@ TOL = {"phi": 2e-5, "rho": 2e-5, "ux": 2e-6, "uy": 2e-6, "uz": 2e-6}
 @pytest.mark.parametrize("bc,tau_g,gravity,noise", [
     (mcb.BC_PERIODIC, 1.0, 0.0, 0.0),
     (mcb.BC_PERIODIC, 0.8, 0.0, 1e-3),
+    (mcb.BC_PERIODIC, 1.0, 1e-4, 1e-3),
+    (mcb.BC_WALLS_Z, 1.0, 0.0, 0.0),
     (mcb.BC_WALLS_Z, 1.0, 1e-4, 0.0),
     (mcb.BC_WALLS_Z, 0.8, 1e-4, 1e-3),
 ])
@@ -66,6 +68,28 @@ def test_f32_matches_fp64_oracle(bc, tau_g, gravity, noise):
     o = oracle_run(cfg, phi, u, steps=30)
     for k, tol in TOL.items():
         assert maxdiff(g, o, k) < tol, (k, maxdiff(g, o, k))
+
+
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
+@pytest.mark.parametrize("bc", [mcb.BC_REF, mcb.BC_PERIODIC, mcb.BC_WALLS_Z])
+def test_first_update_reproduces_the_initial_field(bc, storage):
+    """phi of update 0 is the sum of the initial populations, i.e. the initial phi. This
+    checks the stored-population layout of the init, bounced links included."""
+    cfg, phi, u = small_case(bc if bc != mcb.BC_REF else mcb.BC_PERIODIC, noise=1e-3)
+    if bc == mcb.BC_REF:
+        cfg.bc = mcb.BC_REF
+        phi = mcb.fill_phi_bubbles(cfg.nx, cfg.ny, cfg.nz, mcb.BC_REF, 4.0,
+                                   [(10.3, 9.6, 12.2, 5.0)])
+        u = None
+    cfg.storage = storage
+    g = gpu_run(cfg, phi, u, steps=1)
+    want = phi.astype(np.float64)
+    if bc == mcb.BC_REF:  # interior only: the shell shows the zero-gradient copy
+        sl = (slice(1, -1),) * 3
+        g["phi"], want = g["phi"][sl], want[sl]
+    # float32 rounding; 16-bit storage rounds each stored deviation (11 or 8 bits)
+    tol = {mcb.STORE_F32: 3e-7, mcb.STORE_F16: 2e-5, mcb.STORE_BF16: 2e-4}[storage]
+    assert np.max(np.abs(g["phi"] - want)) < tol
 
 
 def off_centre_reference_phi(n, r=8.0):
