@@ -45,18 +45,27 @@ namespace {
 
 // ------------------------------------------------------------------ storage policies --
 
+// Integer weight split of a cell's phi (face and edge parts) and the same parts as floats.
+// The 16-bit g encoding stores each population relative to its part.
+struct GSplit {
+  int wf, we;
+  float ff, fe;
+};
+
 // f float32 absolute, g Q2.30 absolute (32-bit storage).
 struct StF32 {
   using FT = float;
   using GT = int;
-  static constexpr bool kDev = false;
-  static __device__ __forceinline__ float fload(const FT* p) { return __ldg(p); }
+  static constexpr bool kDev = false;   // g decode needs the source cell's phi
+  static constexpr bool kFDev = false;  // f stored as f_l - W_l
+  static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
   static __device__ __forceinline__ GT gload(const GT* p) { return __ldg(p); }
-  template <int L> static __device__ __forceinline__ float f_dec(FT v) { return v; }
-  template <int L> static __device__ __forceinline__ FT f_enc(float f) { return f; }
+  template <int L> static __device__ __forceinline__ float f_raw(FT v) { return v; }
+  template <int L> static __device__ __forceinline__ FT f_put(float f) { return f; }
   template <int L> static __device__ __forceinline__ int g_dec(GT v, int) { return v; }
+  static __device__ __forceinline__ GSplit g_split(int) { return GSplit{0, 0, 0.f, 0.f}; }
   template <int L>
-  static __device__ __forceinline__ GT g_enc(float g, int, int& q) {
+  static __device__ __forceinline__ GT g_put(float g, const GSplit&, int& q) {
     q = __float2int_rn(g * kQ30);
     return q;
   }
@@ -73,10 +82,9 @@ struct HalfOps {
   using T = __half;
   static __device__ __forceinline__ float tof(T v) { return __half2float(v); }
   static __device__ __forceinline__ T fromf(float f) { return __float2half_rn(f); }
-  // Every finite half is a multiple of 2^-24, hence an exact Q2.30 integer.
-  static __device__ __forceinline__ T enc_exact(float d) {
-    return __float2half_rn(fminf(fmaxf(d, -1.875f), 1.875f));
-  }
+  // Every finite half is a multiple of 2^-24, hence an exact Q2.30 integer. Out-of-range
+  // values saturate the same way on encode and decode, so the phi sum stays exact.
+  static __device__ __forceinline__ T enc_exact(float d) { return __float2half_rn(d); }
 };
 
 struct Bf16Ops {
@@ -87,7 +95,6 @@ struct Bf16Ops {
   // rounded to k * 2^-30 with |k| <= 256 first; that value is exact in bfloat16. Larger
   // ones round to a multiple of 2^-29.
   static __device__ __forceinline__ T enc_exact(float d) {
-    d = fminf(fmaxf(d, -1.875f), 1.875f);
     const int k = __float2int_rn(d * kQ30);
     if (k <= 256 && k >= -256) return __float2bfloat16_rn(static_cast<float>(k) * kInvQ30);
     return __float2bfloat16_rn(d);
@@ -102,21 +109,24 @@ struct St16 {
   using FT = typename O::T;
   using GT = typename O::T;
   static constexpr bool kDev = true;
+  static constexpr bool kFDev = true;
   static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
   static __device__ __forceinline__ GT gload(const GT* p) { return __ldg(p); }
-  template <int L> static __device__ __forceinline__ float f_dec(FT v) {
-    return wf(L) + O::tof(v);
-  }
-  template <int L> static __device__ __forceinline__ FT f_enc(float f) {
-    return O::fromf(f - wf(L));
+  template <int L> static __device__ __forceinline__ float f_raw(FT v) { return O::tof(v); }
+  template <int L> static __device__ __forceinline__ FT f_put(float dev) {
+    return O::fromf(dev);
   }
   template <int L> static __device__ __forceinline__ int g_dec(GT v, int psrc) {
     return wsplit<L>(psrc) + __float2int_rn(O::tof(v) * kQ30);
   }
+  static __device__ __forceinline__ GSplit g_split(int p) {
+    const int wf = wsplit_face(p), we = wsplit_edge_of_face(wf);
+    return GSplit{wf, we, __int2float_rn(wf) * kInvQ30, __int2float_rn(we) * kInvQ30};
+  }
   template <int L>
-  static __device__ __forceinline__ GT g_enc(float g, int pself, int& q) {
-    const int w = wsplit<L>(pself);
-    const GT h = O::enc_exact(g - static_cast<float>(w) * kInvQ30);
+  static __device__ __forceinline__ GT g_put(float g, const GSplit& sp, int& q) {
+    const int w = L <= 6 ? sp.wf : sp.we;
+    const GT h = O::enc_exact(g - (L <= 6 ? sp.ff : sp.fe));
     q = w + __float2int_rn(O::tof(h) * kQ30);
     return h;
   }
@@ -221,10 +231,19 @@ __device__ __forceinline__ Tile locate_tile(const StepArgs& a) {
   return t;
 }
 
+// Register budgets, the largest warp counts per SM that compile without spills: 24 for
+// k_collide (80 registers); for k_phi, 40 with 32-bit storage (48 registers) and 32 with
+// the 16-bit decode (64 registers). Both kernels wait on loads, so resident warps hide
+// latency.
+constexpr int kCollideWarpsPerSM = 24;
+template <class S>
+constexpr int phi_warps_per_sm() { return S::kDev ? 32 : 40; }
+
 // ---------------------------------------------------------------- k_phi: g -> phi --
 
 template <class S, int BX, int BY>
-__global__ void __launch_bounds__(BX * BY) k_phi(const StepArgs a) {
+__global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY))
+    k_phi(const StepArgs a) {
   using GT = typename S::GT;
   const Tile t = locate_tile<BX, BY>(a);
   const int nx = t.nx, ny = t.ny, nz = t.nz;
@@ -297,7 +316,8 @@ __global__ void __launch_bounds__(BX * BY) k_phi(const StepArgs a) {
 // ------------------------------------------------------- k_collide: the fused update --
 
 template <class S, bool BGK, int BX, int BY>
-__global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(const StepArgs a) {
+__global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
+    k_collide(const StepArgs a) {
   using FT = typename S::FT;
   using GT = typename S::GT;
   constexpr int NT = BX * BY;
@@ -510,13 +530,16 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
     //   sum c_a c_b feq = rho (cs^2 d_ab + u_a u_b)
     //   sum c_a c_b HeF = (u_a F_b + u_b F_a)/2 - 3/2 (u.F) u_a u_b
     // This uses the 4th-order isotropy of D3Q19.
+    // 16-bit storage holds f_l - W_l: its moments start from those of the weights
+    // (sum W = 1, sum W c_a c_b = d_ab / 3, odd moments 0).
     float f[kQ];
     static_for<0, kQ>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
-      f[L] = S::template f_dec<L>(fr[L]);
+      f[L] = S::template f_raw<L>(fr[L]);
     });
-    float rho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-    float sxx = 0.f, syy = 0.f, szz = 0.f, sxy = 0.f, sxz = 0.f, syz = 0.f;
+    constexpr float m0 = S::kFDev ? 1.0f : 0.0f, m2 = S::kFDev ? 1.0f / 3.0f : 0.0f;
+    float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
+    float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
     static_for<0, kQ>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
       const float v = f[L];
@@ -549,6 +572,8 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
     // with E_l = 1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2. Opposite pairs share Q_l:Pi and flip
     // c.u and c.F.
     const float om = (1.0f - omega) * 4.5f;
+    // Deviation storage writes f*_l - W_l: the -1 folds into the shared term of each pair.
+    constexpr float fshift = S::kFDev ? -1.0f : 0.0f;
     const float R = rho - h;
     const float base = 1.0f - 1.5f * u2;
     // g collision (collisionPhase, src/lbm.cu:290-329):
@@ -559,7 +584,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
 
     float fo[kQ];
     float go[kQ];
-    fo[0] = wf(0) * (base * R - om * tr3);
+    fo[0] = wf(0) * (base * R - om * tr3 + fshift);
     static_for<0, 9>([&](auto KC) {
       constexpr int L = 2 * decltype(KC)::value + 1;
       constexpr int O = L + 1;
@@ -571,7 +596,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
       if constexpr (cx(L) * cy(L) != 0) qp += (2 * cx(L) * cy(L)) * pxy;
       if constexpr (cx(L) * cz(L) != 0) qp += (2 * cx(L) * cz(L)) * pxz;
       if constexpr (cy(L) * cz(L) != 0) qp += (2 * cy(L) * cz(L)) * pyz;
-      const float q = om * qp;
+      const float q = om * qp + fshift;
       const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
       const float rf = 1.5f * cF;
       fo[L] = W * ((e0 + e1) * (R + rf) + q);
@@ -583,7 +608,7 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
 
     static_for<0, kQ>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
-      fout[L * n + idx] = S::template f_enc<L>(fo[L]);
+      fout[L * n + idx] = S::template f_put<L>(fo[L]);
     });
 
     if constexpr (BGK) {
@@ -611,10 +636,11 @@ __global__ void __launch_bounds__(BX * BY, (BX * BY >= 256 ? 2 : 4)) k_collide(c
       (void)rest_in;
     }
     int sumq = 0;
+    const GSplit sp = S::g_split(pc);
     static_for<1, kQ>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
       int q;
-      gout[(L - 1) * n + idx] = S::template g_enc<L>(go[L], pc, q);
+      gout[(L - 1) * n + idx] = S::template g_put<L>(go[L], sp, q);
       sumq += q;
     });
     rest_out[idx] = S::rest_store(pc, sumq);
@@ -704,14 +730,15 @@ __global__ void k_init(const InitArgs a) {
     const float u2 = ux * ux + uy * uy + uz * uz;
     float feq = wf(L) * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
     if (shell) feq = wf(L);
-    f0[L * n + idx] = S::template f_enc<L>(feq);
-    f1[L * n + idx] = S::template f_enc<L>(feq);
+    const float fst = S::kFDev ? feq - wf(L) : feq;
+    f0[L * n + idx] = S::template f_put<L>(fst);
+    f1[L * n + idx] = S::template f_put<L>(fst);
     if constexpr (L == 0) {
       a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
     } else {
       const float geq = wf(L) * a.phi[ci] * (1.0f + 3.0f * cu);
       int q;
-      g0[(L - 1) * n + idx] = S::template g_enc<L>(geq, P, q);
+      g0[(L - 1) * n + idx] = S::template g_put<L>(geq, S::g_split(P), q);
     }
   });
 }
