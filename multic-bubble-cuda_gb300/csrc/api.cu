@@ -16,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mcb.h"
+#include "mcb.h"
 #include "lattice.h"
 #include "solver.h"
 

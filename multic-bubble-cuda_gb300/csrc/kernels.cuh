@@ -426,13 +426,6 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   int* __restrict__ rest_out = a.rest_out + t.cell_off;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
-  auto prefetch_f = [&](int zpl) {
-    prefetch_rows<NT, BX, BY>(tid, reinterpret_cast<const char*>(fin), n * sizeof(FT), kQ,
-                              sizeof(FT), static_cast<long long>(zpl) * nxy, t.xt, t.yt, nx,
-                              ny);
-  };
-  if (t.zb + 1 < nz) prefetch_f(t.zb + 1);
-
   // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
   for (int zpl = t.zb - 2; zpl <= t.zb + 1; ++zpl) {
     issue(zpl);
@@ -446,7 +439,6 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   for (int z = t.zb; z < t.ze; ++z) {
     commit(z + 2);
     if (z + 3 <= t.ze + 1) issue(z + 3);
-    if (z + 2 < nz && z + 2 <= t.ze) prefetch_f(z + 2);
 
     const int zo = z * nxy;
     const int idx = x + yo + zo;

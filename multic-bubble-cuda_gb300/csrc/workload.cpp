@@ -7,7 +7,7 @@
 #include <cstring>
 #include <vector>
 
-#include "../../include/mcb.h"
+#include "mcb.h"
 
 namespace {
 
