@@ -184,6 +184,29 @@ int  mcb_variant_shape(int variant, int* bx, int* by);
 int  mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
                   double* best_mlups);
 
+/* Allocation-free diagnostics over fields the caller keeps on the device.
+ * No counterpart in the reference. It exists for callers that cannot call cudaMalloc:
+ *   - a host code that owns all device memory through its own pool, sized at start-up;
+ *   - a loop that must not risk the device-wide synchronisation cudaFree can imply.
+ * It computes what mcb_diagnostics computes, from:
+ *   - phi, rho, ux, uy, uz: device arrays of nx*ny*nz floats, x fastest;
+ *   - phi_q30: the matching Q2.30 phi, or NULL to take the integer mass from phi.
+ * It enqueues the reduction on `stream` (NULL: the default stream) and waits for the
+ * result. bc = MCB_BC_REF leaves the shell out, as mcb_diagnostics does.
+ * It allocates nothing on the device or the host. Its scratch is one file-scope device
+ * array of 305 records (about 29 KB), fixed whatever the lattice size, and every GPU that
+ * loads the library holds it until exit.
+ * The first call on a device looks up that array's device address. Make that first call
+ * before any stream capture on the device.
+ * All calls share the array. Calls that overlap on the GPU (other host threads, other
+ * streams) race and must be serialised by the caller. No scratch needs clearing: every
+ * block overwrites its own record. Lattices above MCB_DIAG_DEVICE_MAX_CELLS cells are
+ * rejected with MCB_ERR_INVALID. */
+#define MCB_DIAG_DEVICE_MAX_CELLS 2147483647LL
+int  mcb_diagnostics_device(const float* phi, const float* rho, const float* ux,
+                            const float* uy, const float* uz, const int32_t* phi_q30,
+                            int nx, int ny, int nz, int bc, void* stream, mcb_diag* out);
+
 /* ---- initial fields (host side; one generator shared by the GPU path and the tests) ---- */
 
 /* One bubble: centre, radius and ellipsoid semi-axis factors (1,1,1 = sphere). */

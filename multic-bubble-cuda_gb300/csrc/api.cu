@@ -530,6 +530,13 @@ struct Solver {
   }
 };
 
+namespace mcb {
+int report_error(int code, const char* msg) {
+  g_err = msg ? msg : "";
+  return code;
+}
+}  // namespace mcb
+
 struct mcb_handle {
   Solver s;
 };

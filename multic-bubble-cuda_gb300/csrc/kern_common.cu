@@ -1,6 +1,10 @@
 // Diagnostics reduction and the storage dispatch of the update kernels.
 #include <cfloat>
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
 
+#include "mcb.h"
 #include "solver.h"
 
 namespace mcb {
@@ -114,6 +118,65 @@ __global__ void k_diag_final(const DiagArgs a, int nparts) {
   *a.result = r;
 }
 
+// ------------------------------------------ allocation-free diagnostics (new kernels) --
+
+// The reduction of k_diag over caller-owned device fields, with sizes by value. P may be
+// null, in which case the Q2.30 sum is taken from phi.
+__global__ void __launch_bounds__(kDiagThreads)
+    k_diag_fields(int nx, int ny, int nz, int ref, const float* phi_a, const float* rho_a,
+                  const float* ux_a, const float* uy_a, const float* uz_a, const int* p_a,
+                  DiagPartial* partials) {
+  const long long n = static_cast<long long>(nx) * ny * nz;
+  DiagPartial d;
+  diag_zero(d);
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    if (ref) {
+      const int x = static_cast<int>(i % nx);
+      const int y = static_cast<int>((i / nx) % ny);
+      const int z = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+      if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1) continue;
+    }
+    const float phi = phi_a[i];
+    const float rho = rho_a[i];
+    const float ux = ux_a[i];
+    const float uy = uy_a[i];
+    const float uz = uz_a[i];
+    d.mass_q30 += p_a ? p_a[i] : __float2int_rn(phi * 1073741824.0f);
+    const double u2 = static_cast<double>(ux) * ux + static_cast<double>(uy) * uy +
+                      static_cast<double>(uz) * uz;
+    d.ke += 0.5 * static_cast<double>(rho) * u2;
+    d.umax = fmax(d.umax, sqrt(u2));
+    if (phi > 0.99f) { d.rho_in += rho; d.n_in += 1.0; }
+    if (phi < 0.01f) { d.rho_out += rho; d.n_out += 1.0; }
+    if (phi > 0.5f) d.vol_half += 1.0;
+    d.phi_min = fmin(d.phi_min, static_cast<double>(phi));
+    d.phi_max = fmax(d.phi_max, static_cast<double>(phi));
+    if (!isfinite(phi) || !isfinite(rho) || !isfinite(ux) || !isfinite(uy) || !isfinite(uz))
+      d.nonfinite += 1;
+  }
+  for (int off = 16; off > 0; off >>= 1) diag_shfl(d, off);
+  __shared__ DiagPartial warp_part[kDiagThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_part[warp] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DiagPartial b = warp_part[0];
+    for (int w = 1; w < kDiagThreads / 32; ++w) diag_merge(b, warp_part[w]);
+    partials[blockIdx.x] = b;
+  }
+}
+
+// Merges the partials in block order into partials[nparts].
+__global__ void k_diag_fields_final(DiagPartial* partials, int nparts) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  DiagPartial r = partials[0];
+  for (int i = 1; i < nparts; ++i) diag_merge(r, partials[i]);
+  r.mass = static_cast<double>(r.mass_q30) * (1.0 / 1073741824.0);
+  partials[nparts] = r;
+}
+
 }  // namespace
 
 cudaError_t launch_phi(int storage, int variant, const StepArgs& a, cudaStream_t s) {
@@ -154,3 +217,101 @@ cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s) {
 }
 
 }  // namespace mcb
+
+// ------------------------------------------------------ mcb_diagnostics_device (C ABI) --
+//
+// Some callers cannot call cudaMalloc. A host code that owns every byte of device memory
+// through its own pool, sized once at start-up, forbids later allocations. So does a
+// driver loop that must not risk the device-wide synchronisation cudaFree can imply.
+// mcb_diagnostics_device serves them:
+//   - its only scratch is the file-scope array below;
+//   - the caller passes the fields and receives the result;
+//   - nothing is allocated on the device or the host.
+
+// One partial record per reduction block plus the merged result: (304 + 1) records of 96
+// bytes, about 29 KB. It is the maximum, whatever the lattice size, because the reduction
+// grid is fixed. Every GPU that loads this library holds the array until the process
+// exits. All calls share it.
+static __device__ __align__(256) mcb::DiagPartial g_diag_scratch[mcb::kDiagBlocks + 1];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+mcb::DiagPartial* g_scratch_addr[kMaxDevices] = {};
+thread_local char g_dev_err[256];
+
+int dev_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
+  std::snprintf(g_dev_err, sizeof g_dev_err, "%s%s%s", msg, e != cudaSuccess ? ": " : "",
+                e != cudaSuccess ? cudaGetErrorString(e) : "");
+  mcb::report_error(code, g_dev_err);
+  return code;
+}
+
+// Device address of the scratch array on the current device. In host code the array's name
+// is only a host-side stand-in, so the address comes from cudaGetSymbolAddress, once per
+// device, on the first call made with that device current.
+int scratch_on_current_device(mcb::DiagPartial** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return dev_fail(MCB_ERR_CUDA, "cudaGetDevice failed", e);
+  if (dev < 0 || dev >= kMaxDevices) return dev_fail(MCB_ERR_INVALID, "device ordinal >= 64");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_diag_scratch);
+    if (e != cudaSuccess || !p)
+      return dev_fail(MCB_ERR_CUDA, "cudaGetSymbolAddress of the diagnostics scratch failed", e);
+    g_scratch_addr[dev] = static_cast<mcb::DiagPartial*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return MCB_OK;
+}
+
+}  // namespace
+
+extern "C" int mcb_diagnostics_device(const float* phi, const float* rho, const float* ux,
+                                      const float* uy, const float* uz,
+                                      const int32_t* phi_q30, int nx, int ny, int nz, int bc,
+                                      void* stream, mcb_diag* out) {
+  if (!out || !phi || !rho || !ux || !uy || !uz)
+    return dev_fail(MCB_ERR_INVALID, "mcb_diagnostics_device: NULL field or output pointer");
+  if (nx < 1 || ny < 1 || nz < 1)
+    return dev_fail(MCB_ERR_INVALID, "mcb_diagnostics_device: sizes must be >= 1");
+  if (static_cast<long long>(nx) * ny * nz > MCB_DIAG_DEVICE_MAX_CELLS)
+    return dev_fail(MCB_ERR_INVALID,
+                    "mcb_diagnostics_device: more than 2^31-1 cells (MCB_DIAG_DEVICE_MAX_CELLS)");
+  if (bc != MCB_BC_REF && bc != MCB_BC_PERIODIC && bc != MCB_BC_WALLS_Z)
+    return dev_fail(MCB_ERR_INVALID, "mcb_diagnostics_device: unknown boundary mode");
+  mcb::DiagPartial* scratch = nullptr;
+  const int rc = scratch_on_current_device(&scratch);
+  if (rc != MCB_OK) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  mcb::k_diag_fields<<<mcb::kDiagBlocks, mcb::kDiagThreads, 0, s>>>(
+      nx, ny, nz, bc == MCB_BC_REF, phi, rho, ux, uy, uz, phi_q30, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return dev_fail(MCB_ERR_CUDA, "diagnostics launch failed", e);
+  mcb::k_diag_fields_final<<<1, 32, 0, s>>>(scratch, mcb::kDiagBlocks);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return dev_fail(MCB_ERR_CUDA, "diagnostics launch failed", e);
+  mcb::DiagPartial r;
+  e = cudaMemcpyAsync(&r, scratch + mcb::kDiagBlocks, sizeof r, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return dev_fail(MCB_ERR_CUDA, "diagnostics read-back failed", e);
+  out->mass = r.mass;
+  out->mass_q30 = r.mass_q30;
+  out->kinetic = r.ke;
+  out->umax = r.umax;
+  out->n_in = r.n_in;
+  out->n_out = r.n_out;
+  out->rho_in = r.n_in > 0 ? r.rho_in / r.n_in : 0.0;
+  out->rho_out = r.n_out > 0 ? r.rho_out / r.n_out : 0.0;
+  out->dp = (r.n_in > 0 && r.n_out > 0) ? (out->rho_in - out->rho_out) / 3.0 : 0.0;
+  out->vol_half = r.vol_half;
+  out->phi_min = r.phi_min;
+  out->phi_max = r.phi_max;
+  out->finite = r.nonfinite == 0;
+  out->update = -1;
+  if (!out->finite) return dev_fail(MCB_ERR_NUMERIC, "mcb_diagnostics_device: non-finite values");
+  return MCB_OK;
+}

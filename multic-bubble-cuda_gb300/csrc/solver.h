@@ -95,4 +95,7 @@ cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);
 cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s);
 
+// Records msg as the calling thread's mcb_last_error() text; returns code.
+int report_error(int code, const char* msg);
+
 }  // namespace mcb

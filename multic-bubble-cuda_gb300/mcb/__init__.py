@@ -34,7 +34,7 @@ EXPORTS = [
     "mcb_variant_count", "mcb_variant_shape", "mcb_autotune", "mcb_fill_phi_reference",
     "mcb_fill_phi_bubbles", "mcb_workload", "mcb_batch_create", "mcb_batch_destroy",
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
-    "mcb_batch_last_step_ms", "mcb_batch_cells",
+    "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
 ]
 
 
@@ -121,6 +121,8 @@ def lib() -> C.CDLL:
             "mcb_batch_diagnostics": [vp, C.c_int, C.POINTER(Diag)],
             "mcb_batch_last_step_ms": [vp, _FP],
             "mcb_batch_cells": [vp, C.POINTER(C.c_int64)],
+            "mcb_diagnostics_device": [vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, vp, C.POINTER(Diag)],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -190,6 +192,18 @@ def write_info_file(directory: str, sim_id: str, velocity_set: str, nx: int, ny:
     _check(lib().mcb_write_info_file(directory.encode(), sim_id.encode(), velocity_set.encode(),
                                      nx, ny, nz, tau, umax, fx, fy, fz, save_every, nsteps,
                                      mlups))
+
+
+def diagnostics_device(phi, rho, ux, uy, uz, nx: int, ny: int, nz: int, bc: int,
+                       phi_q30=None, stream=None, allow_nonfinite: bool = False) -> dict:
+    """mcb_diagnostics_device over caller-owned device arrays, given as raw device
+    addresses (ints). The call allocates nothing; see include/mcb.h."""
+    d = Diag()
+    rc = lib().mcb_diagnostics_device(phi, rho, ux, uy, uz, phi_q30, nx, ny, nz, bc, stream,
+                                      C.byref(d))
+    if rc != OK and not (allow_nonfinite and rc == ERR_NUMERIC):
+        _check(rc)
+    return d.as_dict()
 
 
 def workload(scenario: int, case_index: int = 0, seed: int = 1, scale: float = 1.0,
