@@ -226,6 +226,60 @@ def reference_cuda_run(device, steps):
             "steps": steps}
 
 
+def batch_run(device, steps, ncases=64):
+    """64 uneven static/oscillating cases (edges 32..96, FP16 storage) in one launch per
+    phase over the packed case table, graph-replayed. Compared with the same cases run one
+    after another, each with its own handle."""
+    import mcb
+
+    cases = [mcb.workload(4, case_index=i, seed=SEED) for i in range(ncases)]
+    cfgs = []
+    for c, *_ in cases:
+        c.device = device
+        cfgs.append(c)
+    warm = 2 * 16 + 2  # builds both graph parities outside the timed call
+    with mcb.Batch(cfgs) as b:
+        for i, (_, phi, *_r) in enumerate(cases):
+            b.set_fields(i, phi)
+        b.step(warm)
+        b.step(steps)
+        ms_batch = b.last_step_ms()
+        cells = b.cells
+    ms_seq = 0.0
+    for c, (_, phi, *_r) in zip(cfgs, cases):
+        with mcb.Solver(c) as s:
+            s.set_fields(phi)
+            s.step(warm)
+            s.step(steps)
+            ms_seq += s.last_step_ms()
+    return {"cases": ncases, "cells": cells, "storage": "f16", "steps": steps,
+            "batch_mlups": cells * steps / (ms_batch * 1e-3) / 1e6,
+            "sequential_mlups": cells * steps / (ms_seq * 1e-3) / 1e6,
+            "speedup": ms_seq / ms_batch}
+
+
+def swarm_run(device, steps):
+    """The large swarm: 512^3, FP16 storage, walls in z, gravity 5e-6, 512 bubbles."""
+    import mcb
+
+    cfg, phi, *_ = mcb.workload(5, seed=SEED)
+    cfg.device = device
+    cells = cfg.nx * cfg.ny * cfg.nz
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi)
+        s.step(2)
+        m0 = s.diagnostics()["mass_q30"]
+        total, t_phi, t_col = s.step_profiled(steps)
+        d = s.diagnostics()
+    per_update = total * 1e-3 / steps
+    footprint = cells * (2 * 19 * 2 + 2 * (18 * 2 + 4) + 2 * 4 + 5 * 4 + 4 * 4)
+    return {"cells": cells, "storage": "f16", "steps": steps,
+            "mlups": cells / per_update / 1e6,
+            "hbm_gbs_algorithmic": BYTES_PER_LU["f16"] * cells / per_update / 1e9,
+            "mass_drift_q30": int(d["mass_q30"] - m0), "footprint_gb": footprint / 1e9,
+            "kernel_ms": {"k_phi": t_phi / steps, "k_collide": t_col / steps}}
+
+
 def cpu_baseline(seconds=10.0, threads=None):
     """FP64 oracle on the host cores: the scenario at half scale (64x64x128)."""
     import mcb
@@ -302,6 +356,8 @@ def main():
                     help="length scale of the workload (profiling runs use a smaller case)")
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"],
                     help="population storage of the device leg (the headline is f32)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-cases and 512^3 swarm legs")
     ap.add_argument("--only-device", action="store_true",
                     help="time the device loop only (no fp16, e2e, reference or CPU legs)")
     args = ap.parse_args()
@@ -368,6 +424,9 @@ def main():
                           / 1e9 / hbm,
                           "kernel_ms": {"k_phi": p16 / args.steps, "k_collide": c16 / args.steps}}
         result["e2e"] = e2e_run(local, args.steps)
+        if not args.no_extras:
+            result["batch"] = batch_run(local, min(args.steps, 200))
+            result["swarm"] = swarm_run(local, min(args.steps, 50))
         result["reference_cuda"] = reference_cuda_run(local, min(args.steps, 200))
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         print(json.dumps(result))

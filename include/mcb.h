@@ -227,10 +227,13 @@ int  mcb_fill_phi_reference(int nx, int ny, int nz, float r, float width, float*
 int  mcb_fill_phi_bubbles(int nx, int ny, int nz, int bc, float width,
                           const mcb_bubble* bubbles, int nbubbles, float* phi);
 
-/* Seeded workload generator for the five benchmark scenarios (1..5):
+/* Seeded workload generator for the benchmark scenarios:
+ *   0 the reference-parity case: frozen shell, 64^3, the reference's node-centred bubble
+ *     (R 12, width 4), tau 0.8, sigma 0.1;
  *   1 static bubble 64^3; 2 rising perturbed bubble 128x128x256;
  *   3 32 bubbles 256^3 with velocity noise; 4 one case of the batched set (case_index);
- *   5 512 bubbles 512^3.
+ *   5 512 bubbles 512^3; 6 a 64^3 rerun of scenario 3's setting with 4 bubbles.
+ * "Centred" bubbles sit at the geometric centre of the nodes, (n-1)/2.
  * Scale s > 0 multiplies every length (domain, radii, centres) so a scenario can be run
  * smaller; s = 1 is the full size. Writes cfg, then phi/ux/uy/uz if they are non-NULL
  * (nx*ny*nz floats each; call once with NULL to learn the size from cfg). All randomness

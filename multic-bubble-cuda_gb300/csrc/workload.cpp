@@ -225,7 +225,9 @@ int mcb_workload(int scenario, int case_index, uint64_t seed, double scale, mcb_
       cfg->tau = 0.8f;
       cfg->tau_g = 0.8f;
       cfg->sigma = 0.1f;
-      mcb_bubble q{0.5 * e, 0.5 * e, 0.5 * e, 12.0 * scale, 1, 1, 1};
+      // The geometric centre of the node set, (e-1)/2, is off the nodes.
+      const double c = 0.5 * (e - 1);
+      mcb_bubble q{c, c, c, 12.0 * scale, 1, 1, 1};
       bubbles.push_back(q);
       break;
     }
@@ -237,7 +239,7 @@ int mcb_workload(int scenario, int case_index, uint64_t seed, double scale, mcb_
       cfg->tau = 0.7f;
       cfg->sigma = 0.05f;
       cfg->gravity = 1e-5f;
-      mcb_bubble q{0.5 * cfg->nx, 0.5 * cfg->ny, 48.0 * scale, 16.0 * scale, 1, 1, 1};
+      mcb_bubble q{0.5 * (cfg->nx - 1), 0.5 * (cfg->ny - 1), 48.0 * scale, 16.0 * scale, 1, 1, 1};
       bubbles.push_back(q);
       for (int l = 2; l <= 6; ++l) {
         Mode md;
@@ -281,7 +283,8 @@ int mcb_workload(int scenario, int case_index, uint64_t seed, double scale, mcb_
       cfg->tau = static_cast<float>(rng.uniform(0.55, 1.0));
       const double asp = rng.uniform(1.0, 1.3);
       // Volume-preserving prolate ellipsoid along x.
-      mcb_bubble q{0.5 * e, 0.5 * e, 0.5 * e, R, std::pow(asp, 2.0 / 3.0),
+      const double c = 0.5 * (e - 1);
+      mcb_bubble q{c, c, c, R, std::pow(asp, 2.0 / 3.0),
                    std::pow(asp, -1.0 / 3.0), std::pow(asp, -1.0 / 3.0)};
       bubbles.push_back(q);
       break;
@@ -299,6 +302,20 @@ int mcb_workload(int scenario, int case_index, uint64_t seed, double scale, mcb_
       const bool per[3] = {true, true, false};
       if (!place(rng, 512, 5.0 * scale, 10.0 * scale, lo, hi, dims, per, W, bubbles))
         return MCB_ERR_INVALID;
+      break;
+    }
+    case 6: {  // 64^3 periodic rerun of the multi-bubble precision study (4 bubbles)
+      const int e = scaled(64, scale);
+      cfg->nx = cfg->ny = cfg->nz = e;
+      cfg->bc = MCB_BC_PERIODIC;
+      cfg->tau = 0.6f;
+      cfg->sigma = 0.05f;
+      const double lo[3] = {0, 0, 0}, hi[3] = {1.0 * e, 1.0 * e, 1.0 * e};
+      const int dims[3] = {e, e, e};
+      const bool per[3] = {true, true, true};
+      if (!place(rng, 4, 6.0 * scale, 12.0 * scale, lo, hi, dims, per, W, bubbles))
+        return MCB_ERR_INVALID;
+      noise = 1e-4;
       break;
     }
     default:

@@ -1,0 +1,125 @@
+"""Physics known-answers of the CUDA solver, and its 16-bit storage against the FP64 oracle.
+
+The static bubble is the first benchmark config: 64^3 periodic, R 12 at the domain centre,
+W 4, tau 0.8, sigma 0.1, tau_g 0.8, 2000 updates. It checks:
+  - the Laplace law dp = 2 sigma / R, with R the radius of the phi > 1/2 volume;
+  - exact phi-mass conservation;
+  - FP16/BF16 storage against the FP64 oracle: Laplace dp within 2 %, max phi error <= 1e-3.
+The precision-study rerun is a 64^3 periodic box with 4 bubbles, velocity noise, 1000
+updates. It compares every storage with the oracle in phi, u and p.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import mcb
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+STORAGES = {"f32": mcb.STORE_F32, "f16": mcb.STORE_F16, "bf16": mcb.STORE_BF16}
+RESULTS = os.environ.get("MCB_PHYSICS_RESULTS")  # optional JSON dump of the measured numbers
+
+
+def _run_gpu(cfg, fields, steps, storage):
+    cfg.storage = storage
+    with mcb.Solver(cfg) as s:
+        s.set_fields(*fields)
+        s.step(1)
+        m0 = s.diagnostics()["mass_q30"]
+        s.step(steps - 1)
+        d = s.diagnostics()
+        out = {k: s.get(k).astype(np.float64) for k in ("phi", "ux", "uy", "uz", "p")}
+    return out, d, m0
+
+
+def _run_oracle(cfg, fields, steps):
+    o = Oracle.from_config(cfg)
+    o.set_fields(*fields)
+    o.step(steps)
+    return {k: o.get(k) for k in ("phi", "ux", "uy", "uz", "p")}, o.diagnostics()
+
+
+def _dump(name, data):
+    if RESULTS:
+        path = f"{RESULTS}_{name}.json"
+        with open(path, "w") as fp:
+            json.dump(data, fp, indent=1)
+
+
+def test_laplace_law_and_16bit_storage_on_the_static_bubble():
+    cfg, phi, ux, uy, uz = mcb.workload(1)
+    fields = (phi, ux, uy, uz)
+    steps = 2000
+    ref, dref = _run_oracle(cfg, fields, steps)
+    r_ref = (3 * dref["vol_half"] / (4 * math.pi)) ** (1 / 3)
+    report = {"oracle": {"dp": dref["dp"], "R_half": r_ref,
+                         "laplace_err": dref["dp"] * r_ref / (2 * cfg.sigma) - 1}}
+    for name, st in STORAGES.items():
+        g, d, m0 = _run_gpu(cfg, fields, steps, st)
+        r = (3 * d["vol_half"] / (4 * math.pi)) ** (1 / 3)
+        rep = {
+            "dp": d["dp"], "R_half": r,
+            "laplace_err": d["dp"] * r / (2 * cfg.sigma) - 1,
+            "dp_err_vs_oracle": d["dp"] / dref["dp"] - 1,
+            "max_phi_err": float(np.max(np.abs(g["phi"] - ref["phi"]))),
+            "max_u_err": float(max(np.max(np.abs(g[k] - ref[k])) for k in ("ux", "uy", "uz"))),
+            "max_p_err": float(np.max(np.abs(g["p"] - ref["p"]))),
+            "mass_drift_q30": int(d["mass_q30"] - m0),
+        }
+        report[name] = rep
+        assert rep["mass_drift_q30"] == 0, name
+        assert abs(rep["dp_err_vs_oracle"]) <= 0.02, (name, rep)
+        assert rep["max_phi_err"] <= 1e-3, (name, rep)
+        if name == "f32":
+            assert abs(rep["laplace_err"]) <= 0.02, rep
+            assert rep["max_phi_err"] <= 1e-4, rep
+    _dump("laplace", report)
+    print(json.dumps(report))
+
+
+def test_precision_study_rerun_against_the_oracle():
+    cfg, phi, ux, uy, uz = mcb.workload(6, seed=3)
+    fields = (phi, ux, uy, uz)
+    steps = 1000
+    ref, dref = _run_oracle(cfg, fields, steps)
+    report = {}
+    for name, st in STORAGES.items():
+        g, d, m0 = _run_gpu(cfg, fields, steps, st)
+        report[name] = {
+            "max_phi_err": float(np.max(np.abs(g["phi"] - ref["phi"]))),
+            "max_u_err": float(max(np.max(np.abs(g[k] - ref[k])) for k in ("ux", "uy", "uz"))),
+            "max_p_err": float(np.max(np.abs(g["p"] - ref["p"]))),
+            "mass_drift_q30": int(d["mass_q30"] - m0),
+            "mass_rel_vs_oracle": d["mass"] / dref["mass"] - 1,
+        }
+        assert report[name]["mass_drift_q30"] == 0, name
+    assert report["f32"]["max_phi_err"] <= 1e-4, report
+    assert report["f16"]["max_phi_err"] <= 1e-3, report
+    assert report["bf16"]["max_phi_err"] <= 1e-2, report
+    _dump("precision", report)
+    print(json.dumps(report))
+
+
+def test_command_line_driver_writes_reference_style_output(tmp_path):
+    """mcb_sim keeps the reference's argv (<velocity set> <ID>) and output files."""
+    import subprocess
+
+    exe = mcb.LIB_PATH.parent / "mcb_sim"
+    out = str(tmp_path) + "/"
+    r = subprocess.run([str(exe), "D3Q19", "042", "--scenario", "1", "--scale", "0.25",
+                        "--steps", "20", "--save", "10", "--out", out],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    names = sorted(p.name for p in tmp_path.iterdir())
+    assert names == ["042_info.txt", "042_phi000000.bin", "042_phi000010.bin",
+                     "042_phi000020.bin"]
+    n = 16 ** 3
+    for nm in names[1:]:
+        a = np.fromfile(tmp_path / nm, np.float32)
+        assert a.size == n and np.all(np.isfinite(a)) and 0.3 < a.max() <= 1.1
+    info = (tmp_path / "042_info.txt").read_text()
+    assert "NX: 16" in info and "Precision: float" in info and "MLUPS:" in info
