@@ -301,14 +301,15 @@ def cpu_baseline(seconds=10.0, threads=None):
                       f" {n} updates in {dt:.1f} s"}
 
 
-def traffic_per_launch(cells):
-    """DRAM bytes per collide launch from the committed ncu summary, scaled to the cells."""
+def traffic_per_launch(cells, storage="f32"):
+    """DRAM bytes per collide launch, from the committed ncu capture of this workload
+    (profiles/traffic.json, bytes per cell), times the cells of one launch."""
     p = REPO / "profiles" / "traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
     try:
-        return float(d["collide_f32_dram_bytes_per_cell"]) * cells
+        return float(d[f"collide_{storage}_dram_bytes_per_cell"]) * cells
     except KeyError:
         return None
 
@@ -406,7 +407,7 @@ def main():
                      "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": f"{peak_kind} HBM copy bandwidth",
                      "bytes_per_lu": COLLIDE_BYTES_PER_LU[st],
-                     "traffic": traffic_per_launch(cells),
+                     "traffic": traffic_per_launch(cells, st),
                      "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
                      "update_bytes_per_lu": BYTES_PER_LU[st],
                      "kernel_ms": {"k_phi": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
