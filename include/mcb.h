@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MCB_ABI_VERSION 1
+#define MCB_ABI_VERSION 2
 
 /* status codes */
 #define MCB_OK            0
@@ -82,7 +82,17 @@ typedef struct mcb_config {
     int   variant;      /* kernel tile variant, -1 = default (see mcb_variant_count) */
     int   zchunk;       /* z planes per thread block, 0 = default */
     int   use_graph;    /* 1 = replay updates from a CUDA graph, 0 = plain launches */
+    int   g_mode;       /* how g crosses between updates:
+                           MCB_G_AUTO: with tau_g = 1 every post-collision g population is
+                             the equilibrium W_l (phi + c_l.J) of its cell, so only
+                             J = 3 phi u + sharp_c phi (1 - phi) n is stored and the next
+                             update rebuilds the populations; with tau_g != 1 all 19 are
+                             stored;
+                           MCB_G_POPULATIONS: always store the 19 populations. */
 } mcb_config;
+
+#define MCB_G_AUTO         0
+#define MCB_G_POPULATIONS  1
 
 /* FP64 diagnostics, reduced on the device in a fixed order (deterministic). */
 typedef struct mcb_diag {

@@ -80,6 +80,8 @@ int validate(const mcb_config& c, int index) {
   if (c.variant < -1 || c.variant >= mcb::kNumVariants)
     return fail(MCB_ERR_INVALID, "case %d: variant %d out of range", index, c.variant);
   if (c.zchunk < 0) return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= 0", index);
+  if (c.g_mode != MCB_G_AUTO && c.g_mode != MCB_G_POPULATIONS)
+    return fail(MCB_ERR_INVALID, "case %d: unknown g_mode %d", index, c.g_mode);
   return MCB_OK;
 }
 
@@ -96,7 +98,9 @@ struct Solver {
   std::vector<mcb::CaseDesc> cases;
   long long cells_total = 0, max_cells = 0;
   bool bgk = false;
+  int gmode = mcb::kGPop;
   mcb::CaseDesc* d_cases = nullptr;
+  void* jbuf = nullptr;
   void* f[2] = {nullptr, nullptr};
   void* g[2] = {nullptr, nullptr};
   int* rest[2] = {nullptr, nullptr};
@@ -141,6 +145,8 @@ struct Solver {
       rest[i] = p[i] = nullptr;
     }
     cudaFree(macros);
+    cudaFree(jbuf);
+    jbuf = nullptr;
     cudaFree(stage);
     cudaFree(partials);
     cudaFree(result);
@@ -233,6 +239,9 @@ struct Solver {
     }
     cells_total = off;
     fields_set.assign(n, 0);
+    bool force_pop = false;
+    for (int i = 0; i < n; ++i) force_pop = force_pop || cs[i].g_mode == MCB_G_POPULATIONS;
+    gmode = bgk ? mcb::kGBgk : (force_pop ? mcb::kGPop : mcb::kGEquil);
     MCB_TRY(set_device());
     MCB_CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     MCB_CU(cudaEventCreate(&ev0));
@@ -242,10 +251,14 @@ struct Solver {
     const size_t cb = static_cast<size_t>(cells_total) * sizeof(int);
     for (int i = 0; i < 2; ++i) {
       MCB_CU(cudaMalloc(&f[i], fb));
-      MCB_CU(cudaMalloc(&g[i], gb));
-      MCB_CU(cudaMalloc(&rest[i], cb));
+      if (gmode != mcb::kGEquil) {
+        MCB_CU(cudaMalloc(&g[i], gb));
+        MCB_CU(cudaMalloc(&rest[i], cb));
+      }
       MCB_CU(cudaMalloc(&p[i], cb));
     }
+    if (gmode == mcb::kGEquil)
+      MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * 3 * pop_bytes(storage)));
     MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
     MCB_CU(cudaMalloc(&stage, static_cast<size_t>(max_cells) * 4 * sizeof(float)));
     MCB_CU(cudaMalloc(&partials, sizeof(mcb::DiagPartial) * mcb::kDiagBlocks));
@@ -304,6 +317,7 @@ struct Solver {
     a.p1 = p[1];
     a.macros = macros;
     a.cells_total = cells_total;
+    a.gmode = gmode;
     MCB_CU(mcb::launch_init(storage, a, d.nx, d.ny, d.nz, stream));
     MCB_CU(cudaStreamSynchronize(stream));
     fields_set[ci] = 1;
@@ -324,15 +338,20 @@ struct Solver {
     a.p_prev = p[parity ^ 1];
     a.p_cur = p[parity];
     a.macros = with_macros ? macros : nullptr;
+    a.j = jbuf;
     a.cells_total = cells_total;
     a.first = first;
     return a;
   }
 
+  // Equilibrium storage has no populations before the first collision: its first update
+  // takes phi from the init and runs only the collide kernel.
+  bool skips_phi() const { return gmode == mcb::kGEquil && first; }
+
   int launch_update(bool with_macros) {
     const mcb::StepArgs a = args(with_macros);
-    MCB_CU(mcb::launch_phi(storage, variant, a, stream));
-    MCB_CU(mcb::launch_collide(storage, variant, bgk, a, stream));
+    if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+    MCB_CU(mcb::launch_collide(storage, variant, gmode, a, stream));
     latest_p = parity;
     parity ^= 1;
     first = 0;
@@ -413,9 +432,9 @@ struct Solver {
     MCB_CU(cudaEventRecord(ev0, stream));
     for (int i = 0; i < nsteps; ++i) {
       const mcb::StepArgs a = args(i == nsteps - 1);
-      MCB_CU(mcb::launch_phi(storage, variant, a, stream));
+      if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 1], stream));
-      MCB_CU(mcb::launch_collide(storage, variant, bgk, a, stream));
+      MCB_CU(mcb::launch_collide(storage, variant, gmode, a, stream));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 2], stream));
       latest_p = parity;
       parity ^= 1;
@@ -567,6 +586,7 @@ int mcb_config_default(mcb_config* c) {
   c->variant = -1;
   c->zchunk = 0;
   c->use_graph = 1;
+  c->g_mode = MCB_G_AUTO;
   return MCB_OK;
 }
 
@@ -733,7 +753,10 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   // Save the state the next update reads, so every trial starts from it.
   const int par = s.parity;
   const size_t n = static_cast<size_t>(s.cells_total);
-  const size_t fb = n * 19 * pop_bytes(s.storage), gb = n * 18 * pop_bytes(s.storage);
+  const bool eq = s.gmode == mcb::kGEquil;
+  const size_t fb = n * 19 * pop_bytes(s.storage);
+  // Equilibrium storage keeps J (3 values per cell) in place of g and its rest population.
+  const size_t gb = eq ? n * 3 * pop_bytes(s.storage) : n * 18 * pop_bytes(s.storage);
   void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
   auto free_all = [&]() {
     cudaFree(fs);
@@ -758,15 +781,15 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     cudaError_t e = cudaSuccess;
     if (!restore) {
       if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
-      if (e == cudaSuccess) e = cp(gs, s.g[par], gb);
-      if (e == cudaSuccess) e = cp(rs, s.rest[par], n * 4);
+      if (e == cudaSuccess) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
+      if (e == cudaSuccess && !eq) e = cp(rs, s.rest[par], n * 4);
       if (e == cudaSuccess) e = cp(ps, s.p[0], n * 4);
       if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + n * 4, s.p[1], n * 4);
       if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
     } else {
       if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
-      if (e == cudaSuccess) e = cp(s.g[par], gs, gb);
-      if (e == cudaSuccess) e = cp(s.rest[par], rs, n * 4);
+      if (e == cudaSuccess) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
+      if (e == cudaSuccess && !eq) e = cp(s.rest[par], rs, n * 4);
       if (e == cudaSuccess) e = cp(s.p[0], ps, n * 4);
       if (e == cudaSuccess) e = cp(s.p[1], static_cast<char*>(ps) + n * 4, n * 4);
       if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);

@@ -9,12 +9,12 @@
 
 namespace mcb {
 
-cudaError_t launch_phi_f32(int variant, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_phi_f16(int variant, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_phi_bf16(int variant, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_f32(int variant, bool bgk, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_f16(int variant, bool bgk, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_bf16(int variant, bool bgk, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_phi_f32(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_phi_f16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_phi_bf16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_collide_f32(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_collide_f16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_init_f32(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_f16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_bf16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
@@ -179,21 +179,22 @@ __global__ void k_diag_fields_final(DiagPartial* partials, int nparts) {
 
 }  // namespace
 
-cudaError_t launch_phi(int storage, int variant, const StepArgs& a, cudaStream_t s) {
+cudaError_t launch_phi(int storage, int variant, int gmode, const StepArgs& a,
+                       cudaStream_t s) {
   switch (storage) {
-    case kStF32: return launch_phi_f32(variant, a, s);
-    case kStF16: return launch_phi_f16(variant, a, s);
-    case kStBF16: return launch_phi_bf16(variant, a, s);
+    case kStF32: return launch_phi_f32(variant, gmode, a, s);
+    case kStF16: return launch_phi_f16(variant, gmode, a, s);
+    case kStBF16: return launch_phi_bf16(variant, gmode, a, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_collide(int storage, int variant, bool bgk, const StepArgs& a,
+cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& a,
                            cudaStream_t s) {
   switch (storage) {
-    case kStF32: return launch_collide_f32(variant, bgk, a, s);
-    case kStF16: return launch_collide_f16(variant, bgk, a, s);
-    case kStBF16: return launch_collide_bf16(variant, bgk, a, s);
+    case kStF32: return launch_collide_f32(variant, gmode, a, s);
+    case kStF16: return launch_collide_f16(variant, gmode, a, s);
+    case kStBF16: return launch_collide_bf16(variant, gmode, a, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -56,6 +56,7 @@ struct GSplit {
 struct StF32 {
   using FT = float;
   using GT = int;
+  using JT = float;  // J = 3 phi u + A n (equilibrium mode)
   static constexpr bool kDev = false;   // g decode needs the source cell's phi
   static constexpr bool kFDev = false;  // f stored as f_l - W_l
   static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
@@ -76,6 +77,8 @@ struct StF32 {
   static __device__ __forceinline__ int rest_init(float g0, int) {
     return __float2int_rn(g0 * kQ30);
   }
+  static __device__ __forceinline__ float jload(const JT* p) { return __ldg(p); }
+  static __device__ __forceinline__ JT jput(float v) { return v; }
 };
 
 struct HalfOps {
@@ -108,6 +111,7 @@ template <class O>
 struct St16 {
   using FT = typename O::T;
   using GT = typename O::T;
+  using JT = typename O::T;
   static constexpr bool kDev = true;
   static constexpr bool kFDev = true;
   static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
@@ -141,6 +145,8 @@ struct St16 {
   static __device__ __forceinline__ int rest_init(float g0, int p) {
     return __float2int_rn(g0 * kQ30) - wsplit_rest(p);
   }
+  static __device__ __forceinline__ float jload(const JT* p) { return O::tof(__ldg(p)); }
+  static __device__ __forceinline__ JT jput(float v) { return O::fromf(v); }
 };
 
 using StH16 = St16<HalfOps>;
@@ -313,11 +319,104 @@ __global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY
   }
 }
 
+// ------------------------------------- k_phi_eq: g -> phi when g is stored as (phi, J) --
+
+// Q2.30 value of the post-collision population l of a cell with phi and J: the equilibrium
+// W_l (phi + c_l . J) of the g collision (src/lbm.cu:319-326 with c.J = 3 phi c.u +
+// SHARP_C phi (1 - phi) c.n). The _rn intrinsics keep the compiler from contracting it
+// differently in different places. So the cell itself (for its rest population) and its
+// neighbour (for the pulled population) obtain the same integer, and the phi sum stays
+// exact.
+template <int L>
+__device__ __forceinline__ int q_equil(float phi, float jx, float jy, float jz) {
+  constexpr float kWq = static_cast<float>(wd(L) * 1073741824.0);
+  float cj = 0.f;
+  bool any = false;
+  auto add = [&](int c, float v) {
+    if (c == 0) return;
+    const float t = c > 0 ? v : -v;
+    cj = any ? __fadd_rn(cj, t) : t;
+    any = true;
+  };
+  add(cx(L), jx);
+  add(cy(L), jy);
+  add(cz(L), jz);
+  return __float2int_rn(__fmul_rn(__fadd_rn(phi, cj), kWq));
+}
+
+template <class S, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const StepArgs a) {
+  using JT = typename S::JT;
+  const Tile t = locate_tile<BX, BY>(a);
+  const int nx = t.nx, ny = t.ny, nz = t.nz;
+  const int x = t.xt + static_cast<int>(threadIdx.x);
+  const int y = t.yt + static_cast<int>(threadIdx.y);
+  if (x >= nx || y >= ny) return;
+  const long long n = t.ncell;
+  const JT* __restrict__ jxa = static_cast<const JT*>(a.j) + 3 * t.cell_off;
+  const JT* __restrict__ jya = jxa + n;
+  const JT* __restrict__ jza = jxa + 2 * n;
+  const int* __restrict__ pprev = a.p_prev + t.cell_off;
+  int* __restrict__ pcur = a.p_cur + t.cell_off;
+  const int nxy = nx * ny;
+  const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
+  const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+  const int ym = (y == 0 ? ny - 1 : y - 1) * nx, yo = y * nx;
+  const int yp = (y == ny - 1 ? 0 : y + 1) * nx;
+  const bool shell_xy = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1);
+
+  for (int z = t.zb; z < t.ze; ++z) {
+    const int zo = z * nxy;
+    const int idx = x + yo + zo;
+    int P;
+    if (ref && (shell_xy || z == 0 || z == nz - 1)) {
+      // Shell: zero-gradient copy of the previous update's interior phi.
+      const int xc = clampi(x, 1, nx - 2), yc = clampi(y, 1, ny - 2);
+      const int zc = clampi(z, 1, nz - 2);
+      P = __ldg(pprev + xc + yc * nx + zc * nxy);
+    } else {
+      const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
+      const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
+      const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+      const int p0 = __ldg(pprev + idx);
+      const float phi0 = __int2float_rn(p0) * kInvQ30;
+      const float jx0 = S::jload(jxa + idx), jy0 = S::jload(jya + idx);
+      const float jz0 = S::jload(jza + idx);
+      // Rest population: the cell's phi minus its 18 outgoing populations.
+      P = p0;
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        P -= q_equil<L>(phi0, jx0, jy0, jz0);
+      });
+      // Pulled populations; across a z wall the cell's own opposite population returns.
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr int O = opp(L);
+        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+        if (bounce) {
+          P += q_equil<O>(phi0, jx0, jy0, jz0);
+        } else {
+          const int src = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                          src_of<cx(L)>(xm, x, xp);
+          const float ps = __int2float_rn(__ldg(pprev + src)) * kInvQ30;
+          const float sx = cx(L) != 0 ? S::jload(jxa + src) : 0.f;
+          const float sy = cy(L) != 0 ? S::jload(jya + src) : 0.f;
+          const float sz = cz(L) != 0 ? S::jload(jza + src) : 0.f;
+          P += q_equil<L>(ps, sx, sy, sz);
+        }
+      });
+    }
+    pcur[idx] = P;
+  }
+}
+
 // ------------------------------------------------------- k_collide: the fused update --
 
-template <class S, bool BGK, int BX, int BY>
+template <class S, int GM, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     k_collide(const StepArgs a) {
+  constexpr bool BGK = GM == kGBgk;
+  constexpr bool EQ = GM == kGEquil;
   using FT = typename S::FT;
   using GT = typename S::GT;
   constexpr int NT = BX * BY;
@@ -422,8 +521,10 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   FT* __restrict__ fout = static_cast<FT*>(a.f_out) + t.f_off;
   const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
   GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
-  const int* __restrict__ rest_in = a.rest_in + t.cell_off;
-  int* __restrict__ rest_out = a.rest_out + t.cell_off;
+  const int* __restrict__ rest_in = EQ ? nullptr : a.rest_in + t.cell_off;
+  int* __restrict__ rest_out = EQ ? nullptr : a.rest_out + t.cell_off;
+  using JT = typename S::JT;
+  JT* __restrict__ jout = EQ ? static_cast<JT*>(a.j) + 3 * t.cell_off : nullptr;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
   // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
@@ -474,11 +575,17 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     if (shell) {
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
-      static_for<1, kQ>([&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        gout[(L - 1) * n + idx] = S::template g_shell<L>(pc);
-      });
-      rest_out[idx] = S::rest_shell(pc);
+      if constexpr (EQ) {
+        jout[idx] = S::jput(0.f);
+        jout[n + idx] = S::jput(0.f);
+        jout[2 * n + idx] = S::jput(0.f);
+      } else {
+        static_for<1, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          gout[(L - 1) * n + idx] = S::template g_shell<L>(pc);
+        });
+        rest_out[idx] = S::rest_shell(pc);
+      }
       if (a.macros) {
         const long long T = a.cells_total, o = t.cell_off + idx;
         a.macros[o] = __int2float_rn(pc) * kInvQ30;
@@ -627,15 +734,22 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
       (void)gin;
       (void)rest_in;
     }
-    int sumq = 0;
-    const GSplit sp = S::g_split(pc);
-    static_for<1, kQ>([&](auto LC) {
-      constexpr int L = decltype(LC)::value;
-      int q;
-      gout[(L - 1) * n + idx] = S::template g_put<L>(go[L], sp, q);
-      sumq += q;
-    });
-    rest_out[idx] = S::rest_store(pc, sumq);
+    if constexpr (EQ) {
+      // Equilibrium storage: the 18 populations are W_l (phi + c_l . J), J = 3 phi u + A n.
+      jout[idx] = S::jput(phi3 * ux + A * nc.x);
+      jout[n + idx] = S::jput(phi3 * uy + A * nc.y);
+      jout[2 * n + idx] = S::jput(phi3 * uz + A * nc.z);
+    } else {
+      int sumq = 0;
+      const GSplit sp = S::g_split(pc);
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        int q;
+        gout[(L - 1) * n + idx] = S::template g_put<L>(go[L], sp, q);
+        sumq += q;
+      });
+      rest_out[idx] = S::rest_store(pc, sumq);
+    }
 
     if (a.macros) {
       const long long T = a.cells_total, o = t.cell_off + idx;
@@ -670,8 +784,11 @@ __global__ void k_init(const InitArgs a) {
   const bool ref = bc == kBcRef, walls = bc == kBcWallsZ;
   const bool shell = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 ||
                              z == nz - 1);
+  const bool eq = a.gmode == kGEquil;
   const float phi_self = a.phi[idx];
-  const int P = __float2int_rn(phi_self * kQ30);
+  // Equilibrium storage skips k_phi on the first update, so its phi starts here; the
+  // reference's shell phi starts at 0 (src/var.cu:86).
+  const int P = (eq && shell) ? 0 : __float2int_rn(phi_self * kQ30);
   a.p0[co + idx] = P;
   a.p1[co + idx] = P;
   const float ux_s = a.ux ? a.ux[idx] : 0.f;
@@ -725,7 +842,9 @@ __global__ void k_init(const InitArgs a) {
     const float fst = S::kFDev ? feq - wf(L) : feq;
     f0[L * n + idx] = S::template f_put<L>(fst);
     f1[L * n + idx] = S::template f_put<L>(fst);
-    if constexpr (L == 0) {
+    if (eq) {
+      // no g populations are stored
+    } else if constexpr (L == 0) {
       a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
     } else {
       const float geq = wf(L) * a.phi[ci] * (1.0f + 3.0f * cu);
@@ -738,7 +857,17 @@ __global__ void k_init(const InitArgs a) {
 // ------------------------------------------------------------------------ dispatch --
 
 template <class S>
-cudaError_t phi_variant(int variant, const StepArgs& a, cudaStream_t s) {
+cudaError_t phi_variant(int variant, bool eq, const StepArgs& a, cudaStream_t s) {
+  if (eq) {
+    switch (variant) {
+      case 0: k_phi_eq<S, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
+      case 1: k_phi_eq<S, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
+      case 2: k_phi_eq<S, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
+      case 3: k_phi_eq<S, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
+      default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
   switch (variant) {
     case 0: k_phi<S, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
     case 1: k_phi<S, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
@@ -749,13 +878,13 @@ cudaError_t phi_variant(int variant, const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <class S, bool BGK>
+template <class S, int GM>
 cudaError_t collide_variant(int variant, const StepArgs& a, cudaStream_t s) {
   switch (variant) {
-    case 0: k_collide<S, BGK, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
-    case 1: k_collide<S, BGK, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
-    case 2: k_collide<S, BGK, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
-    case 3: k_collide<S, BGK, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
+    case 0: k_collide<S, GM, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
+    case 1: k_collide<S, GM, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
+    case 2: k_collide<S, GM, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
+    case 3: k_collide<S, GM, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -771,13 +900,18 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
 
 // One storage format per translation unit, so the formats compile in parallel.
 #define MCB_STORAGE_LAUNCHERS(S, suffix)                                                   \
-  cudaError_t launch_phi_##suffix(int variant, const StepArgs& a, cudaStream_t s) {        \
-    return phi_variant<S>(variant, a, s);                                                  \
+  cudaError_t launch_phi_##suffix(int variant, int gmode, const StepArgs& a,               \
+                                  cudaStream_t s) {                                        \
+    return phi_variant<S>(variant, gmode == kGEquil, a, s);                                \
   }                                                                                        \
-  cudaError_t launch_collide_##suffix(int variant, bool bgk, const StepArgs& a,            \
+  cudaError_t launch_collide_##suffix(int variant, int gmode, const StepArgs& a,           \
                                       cudaStream_t s) {                                    \
-    return bgk ? collide_variant<S, true>(variant, a, s)                                   \
-               : collide_variant<S, false>(variant, a, s);                                 \
+    switch (gmode) {                                                                       \
+      case kGPop: return collide_variant<S, kGPop>(variant, a, s);                         \
+      case kGBgk: return collide_variant<S, kGBgk>(variant, a, s);                         \
+      case kGEquil: return collide_variant<S, kGEquil>(variant, a, s);                     \
+      default: return cudaErrorInvalidValue;                                               \
+    }                                                                                      \
   }                                                                                        \
   cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
                                    cudaStream_t s) {                                       \

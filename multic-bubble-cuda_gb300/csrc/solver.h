@@ -9,6 +9,14 @@ namespace mcb {
 enum Bc : int { kBcRef = 0, kBcPeriodic = 1, kBcWallsZ = 2 };
 enum Storage : int { kStF32 = 0, kStF16 = 1, kStBF16 = 2 };
 
+// How g crosses from one update to the next.
+//   kGPop:   19 stored populations, full relaxation (g* = geq).
+//   kGBgk:   19 stored populations, BGK relaxation with tau_g != 1.
+//   kGEquil: full relaxation stores only J = 3 phi u + sharp_c phi (1 - phi) n per cell. Each
+//            post-collision population is the equilibrium W_l (phi + c_l . J) of its source
+//            cell, so the next update rebuilds it from (phi, J) of the source.
+enum GMode : int { kGPop = 0, kGBgk = 1, kGEquil = 2 };
+
 // One case of a launch. A single-case handle has one entry. A batch has one entry per case,
 // and every case keeps its own offsets into the shared population buffers.
 struct CaseDesc {
@@ -43,6 +51,7 @@ struct StepArgs {
   const int* p_prev;   // phi of the previous update, Q2.30
   int* p_cur;          // phi of this update, Q2.30
   float* macros;       // nullptr, or [5][cells_total]: phi, rho, ux, uy, uz
+  void* j;             // kGEquil: [3][ncell] per case at 3 * cell_off (Jx, Jy, Jz)
   long long cells_total;
   int first;           // 1 on the first update after fields were set
 };
@@ -62,6 +71,7 @@ struct InitArgs {
   int* p1;
   float* macros;
   long long cells_total;
+  int gmode;
 };
 
 // Per-block partial sums of the diagnostics reduction.
@@ -88,8 +98,9 @@ constexpr int kDiagBlocks = 304;   // fixed grid: the reduction order never chan
 constexpr int kDiagThreads = 256;
 
 // Kernel launchers (kernels.cu). Each returns the launch status.
-cudaError_t launch_phi(int storage, int variant, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide(int storage, int variant, bool bgk, const StepArgs& a,
+cudaError_t launch_phi(int storage, int variant, int gmode, const StepArgs& a,
+                       cudaStream_t s);
+cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& a,
                            cudaStream_t s);
 cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);

@@ -24,6 +24,7 @@ FIELD_PHI, FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_P = range(6)
 FIELDS = {"phi": FIELD_PHI, "rho": FIELD_RHO, "ux": FIELD_UX, "uy": FIELD_UY, "uz": FIELD_UZ,
           "p": FIELD_P}
 STORAGES = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
+G_AUTO, G_POPULATIONS = 0, 1
 
 # Every symbol include/mcb.h declares.
 EXPORTS = [
@@ -49,7 +50,7 @@ class Config(C.Structure):
                 ("storage", C.c_int), ("tau", C.c_float), ("tau_g", C.c_float),
                 ("sigma", C.c_float), ("width", C.c_float), ("sharp_c", C.c_float),
                 ("gravity", C.c_float), ("device", C.c_int), ("variant", C.c_int),
-                ("zchunk", C.c_int), ("use_graph", C.c_int)]
+                ("zchunk", C.c_int), ("use_graph", C.c_int), ("g_mode", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

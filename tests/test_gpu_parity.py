@@ -228,6 +228,35 @@ def test_batch_matches_single_cases_bitwise():
         assert dg[i]["mass_q30"] == single["diag"]["mass_q30"]
 
 
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
+@pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z, mcb.BC_REF])
+def test_equilibrium_g_storage_matches_stored_populations(bc, storage):
+    """With tau_g = 1 the solver stores J instead of the 19 g populations (g_mode auto).
+    Forcing the populations must give the same update up to rounding, with the phi sum
+    exact either way."""
+    if bc == mcb.BC_REF:
+        cfg = reference_cfg(32)
+        phi, u = off_centre_reference_phi(32), None
+    else:
+        cfg, phi, u = small_case(bc, gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    runs = {}
+    for mode in (mcb.G_AUTO, mcb.G_POPULATIONS):
+        cfg.g_mode = mode
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, *(u if u is not None else (None, None, None)))
+            s.step(1)
+            m0 = s.diagnostics()["mass_q30"]
+            s.step(59)
+            d = s.diagnostics()
+            runs[mode] = {k: s.get(k).astype(np.float64) for k in FIELDS}
+            if bc != mcb.BC_REF:
+                assert d["mass_q30"] == m0, mode
+    tol = {mcb.STORE_F32: 2e-6, mcb.STORE_F16: 1e-3}[storage]
+    for k in FIELDS:
+        assert maxdiff(runs[mcb.G_AUTO], runs[mcb.G_POPULATIONS], k) < tol, k
+
+
 def test_rest_state_is_a_fixed_point():
     n = 16
     cfg = mcb.default_config(nx=n, ny=n, nz=n, bc=mcb.BC_PERIODIC, tau=0.7, tau_g=1.0,

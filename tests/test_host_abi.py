@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(built):
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
     assert sorted(mcb.EXPORTS) == names
-    assert L.mcb_abi_version() == 1
+    assert L.mcb_abi_version() == 2
 
 
 def test_config_default_is_the_reference_case(built):
