@@ -258,7 +258,7 @@ struct Solver {
       MCB_CU(cudaMalloc(&p[i], cb));
     }
     if (gmode == mcb::kGEquil)
-      MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * 3 * pop_bytes(storage)));
+      MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * sizeof(float4)));
     MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
     MCB_CU(cudaMalloc(&stage, static_cast<size_t>(max_cells) * 4 * sizeof(float)));
     MCB_CU(cudaMalloc(&partials, sizeof(mcb::DiagPartial) * mcb::kDiagBlocks));
@@ -755,8 +755,8 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   const size_t n = static_cast<size_t>(s.cells_total);
   const bool eq = s.gmode == mcb::kGEquil;
   const size_t fb = n * 19 * pop_bytes(s.storage);
-  // Equilibrium storage keeps J (3 values per cell) in place of g and its rest population.
-  const size_t gb = eq ? n * 3 * pop_bytes(s.storage) : n * 18 * pop_bytes(s.storage);
+  // Equilibrium storage keeps a (phi, J) record per cell in place of g and its rest.
+  const size_t gb = eq ? n * sizeof(float4) : n * 18 * pop_bytes(s.storage);
   void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
   auto free_all = [&]() {
     cudaFree(fs);

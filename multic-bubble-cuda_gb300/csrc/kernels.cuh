@@ -56,7 +56,6 @@ struct GSplit {
 struct StF32 {
   using FT = float;
   using GT = int;
-  using JT = float;  // J = 3 phi u + A n (equilibrium mode)
   static constexpr bool kDev = false;   // g decode needs the source cell's phi
   static constexpr bool kFDev = false;  // f stored as f_l - W_l
   static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
@@ -77,8 +76,6 @@ struct StF32 {
   static __device__ __forceinline__ int rest_init(float g0, int) {
     return __float2int_rn(g0 * kQ30);
   }
-  static __device__ __forceinline__ float jload(const JT* p) { return __ldg(p); }
-  static __device__ __forceinline__ JT jput(float v) { return v; }
 };
 
 struct HalfOps {
@@ -111,7 +108,6 @@ template <class O>
 struct St16 {
   using FT = typename O::T;
   using GT = typename O::T;
-  using JT = typename O::T;
   static constexpr bool kDev = true;
   static constexpr bool kFDev = true;
   static __device__ __forceinline__ FT fload(const FT* p) { return __ldg(p); }
@@ -145,8 +141,6 @@ struct St16 {
   static __device__ __forceinline__ int rest_init(float g0, int p) {
     return __float2int_rn(g0 * kQ30) - wsplit_rest(p);
   }
-  static __device__ __forceinline__ float jload(const JT* p) { return O::tof(__ldg(p)); }
-  static __device__ __forceinline__ JT jput(float v) { return O::fromf(v); }
 };
 
 using StH16 = St16<HalfOps>;
@@ -346,16 +340,13 @@ __device__ __forceinline__ int q_equil(float phi, float jx, float jy, float jz) 
 
 template <class S, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const StepArgs a) {
-  using JT = typename S::JT;
   const Tile t = locate_tile<BX, BY>(a);
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int x = t.xt + static_cast<int>(threadIdx.x);
   const int y = t.yt + static_cast<int>(threadIdx.y);
   if (x >= nx || y >= ny) return;
-  const long long n = t.ncell;
-  const JT* __restrict__ jxa = static_cast<const JT*>(a.j) + 3 * t.cell_off;
-  const JT* __restrict__ jya = jxa + n;
-  const JT* __restrict__ jza = jxa + 2 * n;
+  // One 16-byte record per cell: phi (as float) and J of the previous update.
+  const float4* __restrict__ rec = static_cast<const float4*>(a.j) + t.cell_off;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
   int* __restrict__ pcur = a.p_cur + t.cell_off;
   const int nxy = nx * ny;
@@ -378,15 +369,12 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
       const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
       const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
       const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
-      const int p0 = __ldg(pprev + idx);
-      const float phi0 = __int2float_rn(p0) * kInvQ30;
-      const float jx0 = S::jload(jxa + idx), jy0 = S::jload(jya + idx);
-      const float jz0 = S::jload(jza + idx);
+      const float4 r0 = __ldg(rec + idx);
       // Rest population: the cell's phi minus its 18 outgoing populations.
-      P = p0;
+      P = __ldg(pprev + idx);
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
-        P -= q_equil<L>(phi0, jx0, jy0, jz0);
+        P -= q_equil<L>(r0.x, r0.y, r0.z, r0.w);
       });
       // Pulled populations; across a z wall the cell's own opposite population returns.
       static_for<1, kQ>([&](auto LC) {
@@ -394,15 +382,12 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
         constexpr int O = opp(L);
         const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
         if (bounce) {
-          P += q_equil<O>(phi0, jx0, jy0, jz0);
+          P += q_equil<O>(r0.x, r0.y, r0.z, r0.w);
         } else {
           const int src = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
                           src_of<cx(L)>(xm, x, xp);
-          const float ps = __int2float_rn(__ldg(pprev + src)) * kInvQ30;
-          const float sx = cx(L) != 0 ? S::jload(jxa + src) : 0.f;
-          const float sy = cy(L) != 0 ? S::jload(jya + src) : 0.f;
-          const float sz = cz(L) != 0 ? S::jload(jza + src) : 0.f;
-          P += q_equil<L>(ps, sx, sy, sz);
+          const float4 r = __ldg(rec + src);
+          P += q_equil<L>(r.x, r.y, r.z, r.w);
         }
       });
     }
@@ -523,8 +508,7 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
   const int* __restrict__ rest_in = EQ ? nullptr : a.rest_in + t.cell_off;
   int* __restrict__ rest_out = EQ ? nullptr : a.rest_out + t.cell_off;
-  using JT = typename S::JT;
-  JT* __restrict__ jout = EQ ? static_cast<JT*>(a.j) + 3 * t.cell_off : nullptr;
+  float4* __restrict__ jout = EQ ? static_cast<float4*>(a.j) + t.cell_off : nullptr;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
   // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
@@ -576,9 +560,7 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
       if constexpr (EQ) {
-        jout[idx] = S::jput(0.f);
-        jout[n + idx] = S::jput(0.f);
-        jout[2 * n + idx] = S::jput(0.f);
+        jout[idx] = make_float4(__int2float_rn(pc) * kInvQ30, 0.f, 0.f, 0.f);
       } else {
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
@@ -736,9 +718,8 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     }
     if constexpr (EQ) {
       // Equilibrium storage: the 18 populations are W_l (phi + c_l . J), J = 3 phi u + A n.
-      jout[idx] = S::jput(phi3 * ux + A * nc.x);
-      jout[n + idx] = S::jput(phi3 * uy + A * nc.y);
-      jout[2 * n + idx] = S::jput(phi3 * uz + A * nc.z);
+      jout[idx] = make_float4(phi, phi3 * ux + A * nc.x, phi3 * uy + A * nc.y,
+                              phi3 * uz + A * nc.z);
     } else {
       int sumq = 0;
       const GSplit sp = S::g_split(pc);
