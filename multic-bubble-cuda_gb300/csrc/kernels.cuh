@@ -314,28 +314,36 @@ __global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY
 }
 
 // ------------------------------------- k_phi_eq: g -> phi when g is stored as (phi, J) --
+//
+// With full g relaxation, the post-collision population l of a cell is the equilibrium
+//   g*_l = W_l (phi + c_l . J),  J = 3 phi u + SHARP_C phi (1 - phi) n
+// (src/lbm.cu:319-326). Its Q2.30 value is stored implicitly as two parts:
+//   - the exact integer weight split w_l(P) of the cell's phi, which sums to P over l;
+//   - q_J(l) = rn(W_l c_l.J 2^30), whose opposite directions are exact negatives.
+// The 18 moving parts of a cell therefore add up to P - w_0(P): the rest population is
+// exactly w_0(P), and the lattice sum of phi is invariant. Each cell keeps one 16-byte
+// record of the update: (P as int bits, Jx, Jy, Jz).
 
-// Q2.30 value of the post-collision population l of a cell with phi and J: the equilibrium
-// W_l (phi + c_l . J) of the g collision (src/lbm.cu:319-326 with c.J = 3 phi c.u +
-// SHARP_C phi (1 - phi) c.n). The _rn intrinsics keep the compiler from contracting it
-// differently in different places. So the cell itself (for its rest population) and its
-// neighbour (for the pulled population) obtain the same integer, and the phi sum stays
-// exact.
+// q_J for direction L (its opposite is the exact negative).
 template <int L>
-__device__ __forceinline__ int q_equil(float phi, float jx, float jy, float jz) {
+__device__ __forceinline__ int qj(float jx, float jy, float jz) {
   constexpr float kWq = static_cast<float>(wd(L) * 1073741824.0);
-  float cj = 0.f;
-  bool any = false;
-  auto add = [&](int c, float v) {
-    if (c == 0) return;
-    const float t = c > 0 ? v : -v;
-    cj = any ? __fadd_rn(cj, t) : t;
-    any = true;
-  };
-  add(cx(L), jx);
-  add(cy(L), jy);
-  add(cz(L), jz);
-  return __float2int_rn(__fmul_rn(__fadd_rn(phi, cj), kWq));
+  // c_l . J with at most two nonzero terms, added without contraction.
+  const float a = cx(L) != 0 ? (cx(L) > 0 ? jx : -jx) : (cy(L) > 0 ? jy : -jy);
+  const float b = cx(L) != 0 ? (cy(L) != 0 ? (cy(L) > 0 ? jy : -jy)
+                                           : (cz(L) != 0 ? (cz(L) > 0 ? jz : -jz) : 0.f))
+                             : (cy(L) != 0 ? (cz(L) != 0 ? (cz(L) > 0 ? jz : -jz) : 0.f)
+                                           : 0.f);
+  const bool two = (cx(L) != 0) + (cy(L) != 0) + (cz(L) != 0) == 2;
+  const float cj = cy(L) == 0 && cx(L) == 0 ? (cz(L) > 0 ? jz : -jz)
+                 : (two ? __fadd_rn(a, b) : a);
+  return __float2int_rn(__fmul_rn(cj, kWq));
+}
+
+// Q2.30 population L of a cell record (P, Jx, Jy, Jz).
+template <int L>
+__device__ __forceinline__ int q_rec(float4 r) {
+  return wsplit<L>(__float_as_int(r.x)) + qj<L>(r.y, r.z, r.w);
 }
 
 template <class S, int BX, int BY>
@@ -345,7 +353,6 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
   const int x = t.xt + static_cast<int>(threadIdx.x);
   const int y = t.yt + static_cast<int>(threadIdx.y);
   if (x >= nx || y >= ny) return;
-  // One 16-byte record per cell: phi (as float) and J of the previous update.
   const float4* __restrict__ rec = static_cast<const float4*>(a.j) + t.cell_off;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
   int* __restrict__ pcur = a.p_cur + t.cell_off;
@@ -356,43 +363,40 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
   const int yp = (y == ny - 1 ? 0 : y + 1) * nx;
   const bool shell_xy = ref && (x == 0 || x == nx - 1 || y == 0 || y == ny - 1);
 
-  for (int z = t.zb; z < t.ze; ++z) {
+  auto cell = [&](int z) -> int {
     const int zo = z * nxy;
     const int idx = x + yo + zo;
-    int P;
     if (ref && (shell_xy || z == 0 || z == nz - 1)) {
       // Shell: zero-gradient copy of the previous update's interior phi.
       const int xc = clampi(x, 1, nx - 2), yc = clampi(y, 1, ny - 2);
       const int zc = clampi(z, 1, nz - 2);
-      P = __ldg(pprev + xc + yc * nx + zc * nxy);
-    } else {
-      const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
-      const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
-      const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
-      const float4 r0 = __ldg(rec + idx);
-      // Rest population: the cell's phi minus its 18 outgoing populations.
-      P = __ldg(pprev + idx);
-      static_for<1, kQ>([&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        P -= q_equil<L>(r0.x, r0.y, r0.z, r0.w);
-      });
-      // Pulled populations; across a z wall the cell's own opposite population returns.
-      static_for<1, kQ>([&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        constexpr int O = opp(L);
-        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
-        if (bounce) {
-          P += q_equil<O>(r0.x, r0.y, r0.z, r0.w);
-        } else {
-          const int src = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
-                          src_of<cx(L)>(xm, x, xp);
-          const float4 r = __ldg(rec + src);
-          P += q_equil<L>(r.x, r.y, r.z, r.w);
-        }
-      });
+      return __ldg(pprev + xc + yc * nx + zc * nxy);
     }
-    pcur[idx] = P;
-  }
+    const int zm = (z == 0 ? nz - 1 : z - 1) * nxy;
+    const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
+    const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+    const float4 r0 = __ldg(rec + idx);
+    int P = wsplit_rest(__float_as_int(r0.x));
+    auto pull = [&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      constexpr int O = opp(L);
+      const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+      if (bounce) {
+        P += q_rec<O>(r0);  // across a z wall the cell's own opposite population returns
+      } else {
+        const int src = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                        src_of<cx(L)>(xm, x, xp);
+        P += q_rec<L>(__ldg(rec + src));
+      }
+    };
+    // Nine records in flight at a time: the compiler may not hoist the second half of the
+    // loads above the first half's arithmetic, which keeps the kernel within its registers.
+    static_for<1, 10>(pull);
+    asm volatile("" ::: "memory");
+    static_for<10, kQ>(pull);
+    return P;
+  };
+  for (int z = t.zb; z < t.ze; ++z) pcur[x + yo + z * nxy] = cell(z);
 }
 
 // ------------------------------------------------------- k_collide: the fused update --
@@ -560,7 +564,7 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
       if constexpr (EQ) {
-        jout[idx] = make_float4(__int2float_rn(pc) * kInvQ30, 0.f, 0.f, 0.f);
+        jout[idx] = make_float4(__int_as_float(pc), 0.f, 0.f, 0.f);
       } else {
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
@@ -718,8 +722,8 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     }
     if constexpr (EQ) {
       // Equilibrium storage: the 18 populations are W_l (phi + c_l . J), J = 3 phi u + A n.
-      jout[idx] = make_float4(phi, phi3 * ux + A * nc.x, phi3 * uy + A * nc.y,
-                              phi3 * uz + A * nc.z);
+      jout[idx] = make_float4(__int_as_float(pc), phi3 * ux + A * nc.x,
+                              phi3 * uy + A * nc.y, phi3 * uz + A * nc.z);
     } else {
       int sumq = 0;
       const GSplit sp = S::g_split(pc);

@@ -12,10 +12,10 @@ enum Storage : int { kStF32 = 0, kStF16 = 1, kStBF16 = 2 };
 // How g crosses from one update to the next.
 //   kGPop:   19 stored populations, full relaxation (g* = geq).
 //   kGBgk:   19 stored populations, BGK relaxation with tau_g != 1.
-//   kGEquil: full relaxation stores only phi and J = 3 phi u + sharp_c phi (1 - phi) n per
-//            cell, one 16-byte record. Each post-collision population is the equilibrium
-//            W_l (phi + c_l . J) of its source cell, so the next update rebuilds it from the
-//            source's record.
+//   kGEquil: full relaxation stores only the Q2.30 phi and J = 3 phi u + sharp_c phi (1 - phi) n
+//            per cell, one 16-byte record. Each post-collision population is the
+//            equilibrium W_l (phi + c_l . J) of its source cell, so the next update rebuilds
+//            it from the source's record.
 enum GMode : int { kGPop = 0, kGBgk = 1, kGEquil = 2 };
 
 // One case of a launch. A single-case handle has one entry. A batch has one entry per case,
@@ -52,7 +52,7 @@ struct StepArgs {
   const int* p_prev;   // phi of the previous update, Q2.30
   int* p_cur;          // phi of this update, Q2.30
   float* macros;       // nullptr, or [5][cells_total]: phi, rho, ux, uy, uz
-  void* j;             // kGEquil: float4 (phi, Jx, Jy, Jz) per cell, at cell_off per case
+  void* j;             // kGEquil: 16-byte (P bits, Jx, Jy, Jz) per cell, at cell_off per case
   long long cells_total;
   int first;           // 1 on the first update after fields were set
 };
