@@ -5,8 +5,8 @@ Workload: the rising perturbed bubble:
   - gravity 1e-5, R 16 at z 48, spherical-harmonic modes l = 2..6;
   - tau 0.7, sigma 0.05, W 4;
   - FP32 storage, seeded synthetic initial field.
-A step is one lattice update of the whole lattice. Inputs exceed L2: the f and g buffers
-read by one update hold 637 MB.
+A step is one lattice update of the whole lattice. Inputs exceed L2: the f populations and
+(phi, J) records one update reads hold 386 MB.
 
   value     MLUPS with the state resident in HBM: cells * K / device time of K updates,
             CUDA events on the solver's stream, max over ranks. An event after every
@@ -41,10 +41,38 @@ sys.path.insert(0, str(REPO / "multic-bubble-cuda_gb300"))
 
 METRIC = "MLUPS and % HBM roofline; FP16-store vs FP32 at fixed Laplace-law error"
 SCENARIO, SEED = 2, 1
-# Algorithmic bytes per lattice update: f and g (19 populations each) read once and written
-# once. The collide kernel moves f in and out and g out; the phi kernel moves g in.
-BYTES_PER_LU = {"f32": 304, "f16": 152, "bf16": 152}
-COLLIDE_BYTES_PER_LU = {"f32": 228, "f16": 114, "bf16": 114}
+# Algorithmic bytes per lattice update and kernel, (phi kernel, collide kernel), each array
+# read or written once per cell.
+#   equilibrium g storage (tau_g = 1, the default): k_phi_eq reads the 16-byte (P, J) record
+#     and writes P (4 B). k_collide reads and writes f (19 populations), reads P and writes
+#     the record. 16-bit storage also reads the previous P, the base of the deviation form.
+#   stored g populations (tau_g != 1): k_phi reads g (18 populations) and the rest
+#     population; k_collide reads and writes f and writes g.
+BYTES = {
+    "equilibrium": {"f32": (20, 172), "f16": (20, 100), "bf16": (20, 100)},
+    "populations": {"f32": (76, 228), "f16": (38, 114), "bf16": (38, 114)},
+}
+
+
+def g_storage(cfg) -> str:
+    import mcb
+
+    return ("equilibrium" if cfg.tau_g == 1.0 and cfg.g_mode != mcb.G_POPULATIONS
+            else "populations")
+
+
+def bytes_per_lu(cfg, storage: str) -> tuple[int, int, int]:
+    """(phi kernel, collide kernel, whole update) algorithmic bytes per lattice update."""
+    ph, col = BYTES[g_storage(cfg)][storage]
+    return ph, col, ph + col
+
+
+def footprint_bytes(cells: int, storage: str, gs: str) -> int:
+    """Device bytes of one solver handle: f ping-pong, g state, phi ping-pong, macros,
+    host-upload staging."""
+    pb = 4 if storage == "f32" else 2
+    g = cells * 16 if gs == "equilibrium" else 2 * cells * (18 * pb + 4)
+    return 2 * cells * 19 * pb + g + 2 * cells * 4 + cells * 5 * 4 + cells * 4 * 4
 
 
 def dist_env():
@@ -136,6 +164,7 @@ class Clocks:
 
 
 SCALE = 1.0
+G_POPULATIONS = False
 
 
 def make_solver(storage: str, device: int):
@@ -144,6 +173,8 @@ def make_solver(storage: str, device: int):
     cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=SCALE)
     cfg.storage = mcb.STORAGES[storage]
     cfg.device = device
+    if G_POPULATIONS:
+        cfg.g_mode = mcb.G_POPULATIONS
     s = mcb.Solver(cfg)
     return s, cfg, (phi, ux, uy, uz)
 
@@ -272,11 +303,12 @@ def swarm_run(device, steps):
         total, t_phi, t_col = s.step_profiled(steps)
         d = s.diagnostics()
     per_update = total * 1e-3 / steps
-    footprint = cells * (2 * 19 * 2 + 2 * (18 * 2 + 4) + 2 * 4 + 5 * 4 + 4 * 4)
-    return {"cells": cells, "storage": "f16", "steps": steps,
+    gs = g_storage(cfg)
+    return {"cells": cells, "storage": "f16", "g_storage": gs, "steps": steps,
             "mlups": cells / per_update / 1e6,
-            "hbm_gbs_algorithmic": BYTES_PER_LU["f16"] * cells / per_update / 1e9,
-            "mass_drift_q30": int(d["mass_q30"] - m0), "footprint_gb": footprint / 1e9,
+            "hbm_gbs_algorithmic": bytes_per_lu(cfg, "f16")[2] * cells / per_update / 1e9,
+            "mass_drift_q30": int(d["mass_q30"] - m0),
+            "footprint_gb": footprint_bytes(cells, "f16", gs) / 1e9,
             "kernel_ms": {"k_phi": t_phi / steps, "k_collide": t_col / steps}}
 
 
@@ -301,7 +333,7 @@ def cpu_baseline(seconds=10.0, threads=None):
                       f" {n} updates in {dt:.1f} s"}
 
 
-def traffic_per_launch(cells, storage="f32"):
+def traffic_per_launch(cells, storage="f32", gs="equilibrium"):
     """DRAM bytes per collide launch, from the committed ncu capture of this workload
     (profiles/traffic.json, bytes per cell), times the cells of one launch."""
     p = REPO / "profiles" / "traffic.json"
@@ -309,7 +341,7 @@ def traffic_per_launch(cells, storage="f32"):
         return None
     d = json.loads(p.read_text())
     try:
-        return float(d[f"collide_{storage}_dram_bytes_per_cell"]) * cells
+        return float(d[gs][f"collide_{storage}_dram_bytes_per_cell"]) * cells
     except KeyError:
         return None
 
@@ -359,11 +391,14 @@ def main():
                     help="population storage of the device leg (the headline is f32)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-cases and 512^3 swarm legs")
+    ap.add_argument("--g-populations", action="store_true",
+                    help="store the 19 g populations instead of the (phi, J) records")
     ap.add_argument("--only-device", action="store_true",
                     help="time the device loop only (no fp16, e2e, reference or CPU legs)")
     args = ap.parse_args()
-    global SCALE
+    global SCALE, G_POPULATIONS
     SCALE = args.scale
+    G_POPULATIONS = args.g_populations
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, ws, rank)
@@ -391,8 +426,10 @@ def main():
     hbm, peak_kind = peaks()
     col_avg_s = col_ms * 1e-3 / args.steps
     st = args.storage
-    achieved = COLLIDE_BYTES_PER_LU[st] * cells / col_avg_s / 1e9
-    update_achieved = BYTES_PER_LU[st] * cells / (total_ms * 1e-3 / args.steps) / 1e9
+    gs = g_storage(cfg)
+    _, col_b, upd_b = bytes_per_lu(cfg, st)
+    achieved = col_b * cells / col_avg_s / 1e9
+    update_achieved = upd_b * cells / (total_ms * 1e-3 / args.steps) / 1e9
     result = {
         "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -401,15 +438,15 @@ def main():
         "config": {"workload": f"rising perturbed bubble {cfg.nx}x{cfg.ny}x{cfg.nz}, walls z, "
                                "gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 "
                                "storage",
-                   "cells": cells, "l2": "inputs larger than L2 (f+g 637 MB per update)",
+                   "cells": cells, "l2": "inputs larger than L2 (f + records 386 MB per update)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
         "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": f"{peak_kind} HBM copy bandwidth",
-                     "bytes_per_lu": COLLIDE_BYTES_PER_LU[st],
-                     "traffic": traffic_per_launch(cells, st),
+                     "bytes_per_lu": col_b, "g_storage": gs,
+                     "traffic": traffic_per_launch(cells, st, gs),
                      "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
-                     "update_bytes_per_lu": BYTES_PER_LU[st],
+                     "update_bytes_per_lu": upd_b,
                      "kernel_ms": {"k_phi": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
         "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
@@ -421,8 +458,8 @@ def main():
         _, t16, p16, c16, d16 = device_run("f16", local, args.steps, args.warmup, None)
         v16 = cells * args.steps / (t16 * 1e-3) / 1e6
         result["fp16"] = {"value": v16, "unit": "MLUPS", "ratio_vs_f32": v16 / (value / ws),
-                          "frac_update": BYTES_PER_LU["f16"] * cells / (t16 * 1e-3 / args.steps)
-                          / 1e9 / hbm,
+                          "frac_update": bytes_per_lu(cfg, "f16")[2] * cells
+                          / (t16 * 1e-3 / args.steps) / 1e9 / hbm,
                           "kernel_ms": {"k_phi": p16 / args.steps, "k_collide": c16 / args.steps}}
         result["e2e"] = e2e_run(local, args.steps)
         if not args.no_extras:

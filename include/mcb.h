@@ -170,6 +170,19 @@ int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_s
                          int nx, int ny, int nz, double tau, double umax, double fx,
                          double fy, double fz, int save_every, int nsteps, double mlups);
 
+/* Checkpoint and restart. No counterpart in the reference, which saves only phi
+ * (src/main.cu:184-189) and so cannot resume. mcb_checkpoint_save writes everything the
+ * next update reads:
+ *   - the populations (or, with equilibrium g storage, the per-cell (phi, J) records);
+ *   - both phi buffers;
+ *   - the fields of the latest update;
+ *   - the update counter, the buffer parity and the buoyancy reference;
+ * together with the configuration. mcb_checkpoint_load restores them into a handle created
+ * with the same size, boundary mode, storage and g mode (MCB_ERR_INVALID otherwise). The
+ * run then continues bit-identically. The file is raw little-endian. */
+int  mcb_checkpoint_save(mcb_handle* h, const char* path);
+int  mcb_checkpoint_load(mcb_handle* h, const char* path);
+
 /* Number of updates run since mcb_set_fields, and the size of one case. */
 int  mcb_get_update(const mcb_handle* h, int* update);
 int  mcb_get_dims(const mcb_handle* h, int* nx, int* ny, int* nz);

@@ -461,6 +461,127 @@ struct Solver {
     return MCB_OK;
   }
 
+  // ---- checkpoint: header + raw device buffers ----
+  struct CkptHeader {
+    char magic[8];
+    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad;
+    long long update;
+    float tau, tau_g, sigma, sharp_c, gravity, phi_mean;
+  };
+
+  // (device pointer, bytes) of every buffer the next update reads, in file order.
+  std::vector<std::pair<void*, size_t>> ckpt_buffers() {
+    const size_t n = static_cast<size_t>(cells_total);
+    std::vector<std::pair<void*, size_t>> v;
+    v.push_back({f[parity], n * 19 * pop_bytes(storage)});
+    if (gmode == mcb::kGEquil) {
+      v.push_back({jbuf, n * sizeof(float4)});
+    } else {
+      v.push_back({g[parity], n * 18 * pop_bytes(storage)});
+      v.push_back({rest[parity], n * sizeof(int)});
+    }
+    v.push_back({p[0], n * sizeof(int)});
+    v.push_back({p[1], n * sizeof(int)});
+    v.push_back({macros, n * 5 * sizeof(float)});
+    return v;
+  }
+
+  int ckpt_save(const char* path) {
+    if (!path) return fail(MCB_ERR_INVALID, "path is NULL");
+    if (cases.size() != 1) return fail(MCB_ERR_INVALID, "checkpoints hold one case");
+    if (!fields_set[0]) return fail(MCB_ERR_STATE, "fields are not set");
+    MCB_TRY(set_device());
+    MCB_CU(cudaStreamSynchronize(stream));
+    CkptHeader hd{};
+    std::memcpy(hd.magic, "MCBCKPT1", 8);
+    const mcb::CaseDesc& d = cases[0];
+    hd.abi = MCB_ABI_VERSION;
+    hd.nx = d.nx;
+    hd.ny = d.ny;
+    hd.nz = d.nz;
+    hd.bc = d.bc;
+    hd.storage = storage;
+    hd.gmode = gmode;
+    hd.parity = parity;
+    hd.first = first;
+    hd.latest_p = latest_p;
+    hd.update = update;
+    hd.tau = cfg[0].tau;
+    hd.tau_g = cfg[0].tau_g;
+    hd.sigma = d.sigma;
+    hd.sharp_c = d.sharp_c;
+    hd.gravity = d.gravity;
+    hd.phi_mean = d.phi_mean;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(MCB_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&hd, sizeof hd, 1, fp) == 1;
+    std::vector<char> buf(64 << 20);
+    for (auto& b : ckpt_buffers()) {
+      for (size_t off = 0; ok && off < b.second; off += buf.size()) {
+        const size_t len = std::min(buf.size(), b.second - off);
+        if (cudaMemcpy(buf.data(), static_cast<char*>(b.first) + off, len,
+                       cudaMemcpyDeviceToHost) != cudaSuccess) {
+          std::fclose(fp);
+          return fail(MCB_ERR_CUDA, "checkpoint read-back failed");
+        }
+        ok = std::fwrite(buf.data(), 1, len, fp) == len;
+      }
+    }
+    if (std::fclose(fp) != 0) ok = false;
+    if (!ok) return fail(MCB_ERR_IO, "short write to %s", path);
+    return MCB_OK;
+  }
+
+  int ckpt_load(const char* path) {
+    if (!path) return fail(MCB_ERR_INVALID, "path is NULL");
+    if (cases.size() != 1) return fail(MCB_ERR_INVALID, "checkpoints hold one case");
+    MCB_TRY(set_device());
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(MCB_ERR_IO, "cannot open %s", path);
+    CkptHeader hd{};
+    if (std::fread(&hd, sizeof hd, 1, fp) != 1 || std::memcmp(hd.magic, "MCBCKPT1", 8) != 0) {
+      std::fclose(fp);
+      return fail(MCB_ERR_INVALID, "%s is not a solver checkpoint", path);
+    }
+    mcb::CaseDesc& d = cases[0];
+    if (hd.nx != d.nx || hd.ny != d.ny || hd.nz != d.nz || hd.bc != d.bc ||
+        hd.storage != storage || hd.gmode != gmode) {
+      std::fclose(fp);
+      return fail(MCB_ERR_INVALID,
+                  "checkpoint %s was written for another size, boundary mode, storage or g mode",
+                  path);
+    }
+    MCB_CU(cudaStreamSynchronize(stream));
+    parity = hd.parity;
+    std::vector<char> buf(64 << 20);
+    bool ok = true;
+    for (auto& b : ckpt_buffers()) {
+      for (size_t off = 0; ok && off < b.second; off += buf.size()) {
+        const size_t len = std::min(buf.size(), b.second - off);
+        ok = std::fread(buf.data(), 1, len, fp) == len;
+        if (ok && cudaMemcpy(static_cast<char*>(b.first) + off, buf.data(), len,
+                             cudaMemcpyHostToDevice) != cudaSuccess) {
+          std::fclose(fp);
+          return fail(MCB_ERR_CUDA, "checkpoint upload failed");
+        }
+      }
+    }
+    std::fclose(fp);
+    if (!ok) return fail(MCB_ERR_IO, "%s is truncated", path);
+    // Reference-mode shells keep f = W_l in both buffers: the other buffer takes the same.
+    const size_t fbytes = static_cast<size_t>(cells_total) * 19 * pop_bytes(storage);
+    MCB_CU(cudaMemcpy(f[parity ^ 1], f[parity], fbytes, cudaMemcpyDeviceToDevice));
+    first = hd.first;
+    latest_p = hd.latest_p;
+    update = hd.update;
+    d.phi_mean = hd.phi_mean;
+    MCB_CU(cudaMemcpy(d_cases, &d, sizeof d, cudaMemcpyHostToDevice));
+    drop_graphs();
+    fields_set[0] = 1;
+    stepped = update >= 0;
+    return MCB_OK;
+  }
+
   int sync() {
     MCB_TRY(set_device());
     MCB_CU(cudaStreamSynchronize(stream));
@@ -707,6 +828,16 @@ int mcb_write_info(const mcb_handle* h, const char* dir, const char* id,
   }
   return mcb_write_info_file(dir, id, velocity_set, c.nx, c.ny, c.nz, c.tau, umax, 0.0, 0.0,
                              c.gravity, save_every, nsteps, mlups);
+}
+
+int mcb_checkpoint_save(mcb_handle* h, const char* path) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.ckpt_save(path);
+}
+
+int mcb_checkpoint_load(mcb_handle* h, const char* path) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.ckpt_load(path);
 }
 
 int mcb_get_update(const mcb_handle* h, int* update) {

@@ -36,6 +36,7 @@ EXPORTS = [
     "mcb_fill_phi_bubbles", "mcb_workload", "mcb_batch_create", "mcb_batch_destroy",
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
     "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
+    "mcb_checkpoint_save", "mcb_checkpoint_load",
 ]
 
 
@@ -102,6 +103,8 @@ def lib() -> C.CDLL:
             "mcb_write_info_file": [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int,
                                     C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_int, C.c_int, C.c_double],
+            "mcb_checkpoint_save": [vp, C.c_char_p],
+            "mcb_checkpoint_load": [vp, C.c_char_p],
             "mcb_get_update": [vp, C.POINTER(C.c_int)],
             "mcb_get_dims": [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
             "mcb_last_step_ms": [vp, _FP],
@@ -282,6 +285,12 @@ class Solver:
                    save_every: int = 100, nsteps: int = 0, mlups: float = 0.0) -> None:
         _check(lib().mcb_write_info(self._h, directory.encode(), sim_id.encode(),
                                     velocity_set.encode(), save_every, nsteps, mlups))
+
+    def checkpoint_save(self, path: str) -> None:
+        _check(lib().mcb_checkpoint_save(self._h, str(path).encode()))
+
+    def checkpoint_load(self, path: str) -> None:
+        _check(lib().mcb_checkpoint_load(self._h, str(path).encode()))
 
     @property
     def update(self) -> int:

@@ -296,6 +296,39 @@ def test_autotune_restores_the_state():
             assert np.array_equal(s.get(k).astype(np.float64), ref[k]), k
 
 
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
+@pytest.mark.parametrize("bc,tau_g", [(mcb.BC_PERIODIC, 1.0), (mcb.BC_WALLS_Z, 0.8),
+                                      (mcb.BC_REF, 1.0)])
+def test_checkpoint_restart_continues_bitwise(tmp_path, bc, tau_g, storage):
+    if bc == mcb.BC_REF:
+        cfg, phi, u = reference_cfg(32), off_centre_reference_phi(32), None
+    else:
+        cfg, phi, u = small_case(bc, tau_g=tau_g, gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    ck = str(tmp_path / "state.ckpt")
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, *(u if u is not None else (None, None, None)))
+        s.step(31)
+        s.checkpoint_save(ck)
+        s.step(23)
+        want = {k: s.get(k) for k in FIELDS}
+        want_d = s.diagnostics()
+    with mcb.Solver(cfg) as s2:
+        s2.checkpoint_load(ck)
+        assert s2.update == 30
+        s2.step(23)
+        assert s2.update == 53
+        for k in FIELDS:
+            assert np.array_equal(s2.get(k), want[k]), k
+        assert s2.diagnostics()["mass_q30"] == want_d["mass_q30"]
+    other = mcb.default_config(nx=cfg.nx + 2, ny=cfg.ny, nz=cfg.nz, bc=cfg.bc, tau=cfg.tau,
+                               tau_g=cfg.tau_g, width=4.0, storage=storage)
+    with mcb.Solver(other) as s3:
+        with pytest.raises(mcb.McbError) as e:
+            s3.checkpoint_load(ck)
+        assert e.value.code == mcb.ERR_INVALID
+
+
 def test_errors_come_back_as_status_codes():
     cfg, phi, _ = small_case(mcb.BC_PERIODIC)
     with mcb.Solver(cfg) as s:
