@@ -80,7 +80,10 @@ typedef struct mcb_config {
     float gravity;      /* Boussinesq buoyancy: F_z += gravity * (phi - mean phi); 0 = off */
     int   device;       /* CUDA device ordinal */
     int   variant;      /* kernel tile variant, -1 = default (see mcb_variant_count) */
-    int   zchunk;       /* z planes per thread block, 0 = default */
+    int   zchunk;       /* work split: > 0 fixed chunks of zchunk z planes per block;
+                           -w (w <= 16) balanced over w waves of resident blocks, each
+                           block taking an equal run of planes; 0 = default (balanced
+                           with (phi, J) records, fixed chunks otherwise) */
     int   use_graph;    /* 1 = replay updates from a CUDA graph, 0 = plain launches */
     int   g_mode;       /* how g crosses between updates:
                            MCB_G_AUTO: with tau_g = 1 every post-collision g population is
@@ -153,6 +156,12 @@ int  mcb_diagnostics(mcb_handle* h, mcb_diag* out);
  * x fastest. post/fileTreat.py reads the file back. dir must end in a path separator,
  * as SIM_DIR does in src/main.cu:20-21. */
 int  mcb_dump_phi(mcb_handle* h, const char* dir, const char* id, int step);
+
+/* The same dump for any field of mcb_get_field: "<dir><id>_<name>%06d.bin", with name
+ * phi, rho, ux, uy, uz or pres (p = rho/3; "pres" because post/fileTreat.py matches
+ * file names by substring, and "p" is a substring of "phi"). The reference dumps phi
+ * only; post/fileTreat.py:8 reads the others once they are added to __macr_names__. */
+int  mcb_dump_field(mcb_handle* h, const char* dir, const char* id, int which, int step);
 
 /* Replaces generateSimulationInfoFile (src/auxFunctions.cu:12-47): writes
  * "<dir><id>_info.txt" in the layout post/fileTreat.py:37-124 parses, with

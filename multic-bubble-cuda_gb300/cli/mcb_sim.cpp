@@ -21,8 +21,13 @@
 //   --seed N        scenario seed (default 1)
 //   --storage f32|f16|bf16
 //   --autotune      pick the fastest tile variant before running
+//   --fields LIST   comma-separated fields to dump: phi,rho,ux,uy,uz,pres (default phi)
+//   --checkpoint F  write a checkpoint of the full solver state to F after the last update
+//   --restart F     resume from checkpoint F (same case options) instead of the initial
+//                   fields; updates already run are not repeated
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <chrono>
 #include <cstdio>
@@ -68,6 +73,8 @@ int main(int argc, char** argv) {
   unsigned long long seed = 1;
   int storage = -1;
   std::string out = "../bin/" + vs + "/" + id + "/";
+  std::string checkpoint, restart;
+  std::vector<int> fields = {MCB_FIELD_PHI};
   for (int i = 3; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> const char* {
@@ -84,6 +91,27 @@ int main(int argc, char** argv) {
     else if (a == "--scale") scale = std::atof(next());
     else if (a == "--seed") seed = std::strtoull(next(), nullptr, 10);
     else if (a == "--autotune") autotune = 1;
+    else if (a == "--checkpoint") checkpoint = next();
+    else if (a == "--restart") restart = next();
+    else if (a == "--fields") {
+      static const char* const names[] = {"phi", "rho", "ux", "uy", "uz", "pres"};
+      fields.clear();
+      std::string list = next();
+      size_t pos = 0;
+      while (pos <= list.size()) {
+        const size_t end = std::min(list.find(',', pos), list.size());
+        const std::string name = list.substr(pos, end - pos);
+        int k = -1;
+        for (int j = 0; j < 6; ++j)
+          if (name == names[j]) k = j;
+        if (k < 0) {
+          std::fprintf(stderr, "mcb_sim: unknown field %s\n", name.c_str());
+          return 1;
+        }
+        fields.push_back(k);
+        pos = end + 1;
+      }
+    }
     else if (a == "--storage") {
       const std::string s = next();
       storage = s == "f32" ? MCB_STORE_F32 : s == "f16" ? MCB_STORE_F16
@@ -136,6 +164,12 @@ int main(int argc, char** argv) {
   if ((rc = mcb_set_fields(h, phi.data(), ux.empty() ? nullptr : ux.data(),
                            uy.empty() ? nullptr : uy.data(), uz.empty() ? nullptr : uz.data())))
     return die("mcb_set_fields", rc);
+  int done = -1;  // last update run
+  if (!restart.empty()) {
+    if ((rc = mcb_checkpoint_load(h, restart.c_str()))) return die("mcb_checkpoint_load", rc);
+    if ((rc = mcb_get_update(h, &done))) return die("mcb_get_update", rc);
+    std::printf("restart: %s after update %d\n", restart.c_str(), done);
+  }
   if (autotune) {
     int v = 0, zc = 0;
     double ml = 0;
@@ -147,7 +181,7 @@ int main(int argc, char** argv) {
 
   double device_ms = 0.0;
   const auto t0 = std::chrono::steady_clock::now();
-  int done = -1;  // last update run
+  const int first_update = done + 1;
   auto advance = [&](int target) -> int {
     const int n = target - done;
     if (n <= 0) return 0;
@@ -159,10 +193,15 @@ int main(int argc, char** argv) {
     done = target;
     return 0;
   };
-  for (int s = 0; s <= nsteps;) {
+  // First dump point after a restart: the next multiple of save past the restored update.
+  int s0 = 0;
+  if (done >= 0) s0 = save > 0 ? std::min((done / save + 1) * save, nsteps) : nsteps;
+  for (int s = s0; s <= nsteps && done < nsteps;) {
     if ((rc = advance(s))) return die("mcb_step", rc);
     if (save > 0 && s % save == 0) {
-      if ((rc = mcb_dump_phi(h, out.c_str(), id.c_str(), s))) return die("mcb_dump_phi", rc);
+      for (int k : fields)
+        if ((rc = mcb_dump_field(h, out.c_str(), id.c_str(), k, s)))
+          return die("mcb_dump_field", rc);
     }
     if (s == nsteps) break;
     const int nxt = save > 0 ? (s / save + 1) * save : nsteps;
@@ -170,7 +209,7 @@ int main(int argc, char** argv) {
   }
   const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   const double cells = static_cast<double>(cfg.nx) * cfg.ny * cfg.nz;
-  const double updates = nsteps + 1.0;
+  const double updates = static_cast<double>(nsteps + 1 - first_update);
   const double mlups_dev = device_ms > 0 ? cells * updates / (device_ms * 1e-3) / 1e6 : 0.0;
   const double mlups_wall = wall > 0 ? cells * updates / wall / 1e6 : 0.0;
   mcb_diag d;
@@ -178,8 +217,10 @@ int main(int argc, char** argv) {
   if (rc && rc != MCB_ERR_NUMERIC) return die("mcb_diagnostics", rc);
   if ((rc = mcb_write_info(h, out.c_str(), id.c_str(), vs.c_str(), save, nsteps, mlups_dev)))
     return die("mcb_write_info", rc);
+  if (!checkpoint.empty() && (rc = mcb_checkpoint_save(h, checkpoint.c_str())))
+    return die("mcb_checkpoint_save", rc);
   std::printf("updates %d  cells %.0f  device %.3f s  %.1f MLUPS (device)  %.1f MLUPS (wall)\n",
-              nsteps + 1, cells, device_ms * 1e-3, mlups_dev, mlups_wall);
+              static_cast<int>(updates), cells, device_ms * 1e-3, mlups_dev, mlups_wall);
   std::printf("mass %.12e  kinetic %.6e  umax %.6e  dp %.6e  finite %d\n", d.mass, d.kinetic,
               d.umax, d.dp, d.finite);
   mcb_destroy(h);

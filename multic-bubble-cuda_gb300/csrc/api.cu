@@ -48,6 +48,12 @@ int fail(int code, const char* fmt, ...) {
     if (r_ != MCB_OK) return r_; \
   } while (0)
 
+// Balanced work decomposition: resident waves of equal-work blocks per kernel. One wave
+// has no tail: every block of the launch finishes at the same time.
+constexpr int kDefaultWaves = 1;
+constexpr int kMaxWaves = 16;
+constexpr int kMinCollidePlanes = 8;
+
 size_t pop_bytes(int storage) { return storage == mcb::kStF32 ? 4 : 2; }
 
 int validate(const mcb_config& c, int index) {
@@ -79,7 +85,8 @@ int validate(const mcb_config& c, int index) {
     return fail(MCB_ERR_INVALID, "case %d: non-finite parameter", index);
   if (c.variant < -1 || c.variant >= mcb::kNumVariants)
     return fail(MCB_ERR_INVALID, "case %d: variant %d out of range", index, c.variant);
-  if (c.zchunk < 0) return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= 0", index);
+  if (c.zchunk < -kMaxWaves)
+    return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= -%d", index, kMaxWaves);
   if (c.g_mode != MCB_G_AUTO && c.g_mode != MCB_G_POPULATIONS)
     return fail(MCB_ERR_INVALID, "case %d: unknown g_mode %d", index, c.g_mode);
   return MCB_OK;
@@ -114,6 +121,7 @@ struct Solver {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_steps = 16;
   int ntiles = 0, zchunk = 16;
+  int balanced = 1, planes = 0, grid_phi = 0, grid_collide = 0;
   int parity = 0, first = 1, latest_p = 1;
   long long update = -1;
   std::vector<char> fields_set;
@@ -163,37 +171,67 @@ struct Solver {
     stream = nullptr;
   }
 
-  // Tile decomposition of every case for the current variant and z chunk.
+  // Work decomposition of every case for the current variant and z chunk request:
+  //   zchunk_req > 0: fixed chunks of that many planes, one block each;
+  //   zchunk_req < 0: balanced ranges, -zchunk_req resident waves of equal-work blocks
+  //   per kernel;
+  //   zchunk_req == 0: balanced over kDefaultWaves with equilibrium g storage; fixed
+  //   chunks otherwise (measured on GB300 at 128x128x256: balanced ranges are 2 % faster
+  //   with (P, J) records at FP16 and equal at FP32, while the stored-population phi
+  //   kernel is 25 % slower with them than with 16-plane chunks).
   int build_tiles() {
     const mcb::Variant v = mcb::kVariants[variant];
+    long long plane_total = 0;
+    for (auto& d : cases) {
+      d.tiles_x = (d.nx + v.bx - 1) / v.bx;
+      d.tiles_y = (d.ny + v.by - 1) / v.by;
+      d.plane0 = static_cast<int>(plane_total);
+      plane_total += static_cast<long long>(d.tiles_x) * d.tiles_y * d.nz;
+      if (plane_total > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tile planes");
+    }
+    planes = static_cast<int>(plane_total);
+    balanced = zchunk_req < 0 || (zchunk_req == 0 && gmode == mcb::kGEquil);
     auto tiles_for = [&](int zc) {
       long long total = 0;
-      for (auto& c : cfg)
-        total += static_cast<long long>((c.nx + v.bx - 1) / v.bx) * ((c.ny + v.by - 1) / v.by) *
-                 ((c.nz + zc - 1) / zc);
+      for (auto& d : cases)
+        total += static_cast<long long>(d.tiles_x) * d.tiles_y * ((d.nz + zc - 1) / zc);
       return total;
     };
     int zc = zchunk_req;
     if (zc <= 0) {
-      // Aim for at least three waves of two blocks per SM on 152 SMs; longer z chunks
-      // amortise the halo planes of the march (measured best: 16 planes at 128x128x256).
+      // Fixed-chunk default: at least three waves of two blocks per SM on 152 SMs; longer
+      // chunks amortise the halo planes of the march (measured best: 16 planes at
+      // 128x128x256).
       zc = 32;
       while (zc > 4 && tiles_for(zc) < 3LL * 2 * 152) zc /= 2;
     }
-    const long long total = tiles_for(zc);
-    if (total > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tiles (%lld)", total);
-    zchunk = zc;
-    int tile0 = 0;
-    for (size_t i = 0; i < cases.size(); ++i) {
-      mcb::CaseDesc& d = cases[i];
-      d.tiles_x = (d.nx + v.bx - 1) / v.bx;
-      d.tiles_y = (d.ny + v.by - 1) / v.by;
+    const long long tile0_total = tiles_for(zc);
+    if (tile0_total > 0x7fffffffLL)
+      return fail(MCB_ERR_INVALID, "too many tiles (%lld)", tile0_total);
+    long long tile0 = 0;
+    for (auto& d : cases) {
       d.zchunk = zc;
       d.tiles_z = (d.nz + zc - 1) / zc;
-      d.tile0 = tile0;
-      tile0 += d.tiles_x * d.tiles_y * d.tiles_z;
+      d.tile0 = static_cast<int>(tile0);
+      tile0 += static_cast<long long>(d.tiles_x) * d.tiles_y * d.tiles_z;
     }
-    ntiles = tile0;
+    ntiles = static_cast<int>(tile0);
+    zchunk = balanced ? (zchunk_req < 0 ? zchunk_req : -kDefaultWaves) : zc;
+    if (balanced) {
+      const int waves = -zchunk;
+      int nsm = 0, occ_phi = 0, occ_col = 0;
+      MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+      MCB_CU(mcb::occupancy(storage, variant, gmode, &occ_phi, &occ_col));
+      if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
+        return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
+      grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
+      // A collide piece re-reads four phi planes and recomputes two normal planes before
+      // its first plane: give each block at least kMinCollidePlanes.
+      grid_collide = static_cast<int>(std::min<long long>(
+          std::max(1, planes / kMinCollidePlanes), 1LL * occ_col * nsm * waves));
+    } else {
+      grid_phi = grid_collide = ntiles;
+    }
     drop_graphs();
     MCB_CU(cudaMemcpyAsync(d_cases, cases.data(), sizeof(mcb::CaseDesc) * cases.size(),
                            cudaMemcpyHostToDevice, stream));
@@ -330,6 +368,10 @@ struct Solver {
     a.cases = d_cases;
     a.ncases = static_cast<int>(cases.size());
     a.ntiles = ntiles;
+    a.balanced = balanced;
+    a.planes = planes;
+    a.grid_phi = grid_phi;
+    a.grid_collide = grid_collide;
     a.f_in = f[parity];
     a.f_out = f[parity ^ 1];
     a.g_in = g[parity];
@@ -817,6 +859,18 @@ int mcb_dump_phi(mcb_handle* h, const char* dir, const char* id, int step) {
   return mcb_write_phi_file(dir, id, "phi", step, buf.data(), buf.size());
 }
 
+int mcb_dump_field(mcb_handle* h, const char* dir, const char* id, int which, int step) {
+  static const char* const kNames[] = {"phi", "rho", "ux", "uy", "uz", "pres"};
+  if (!h || !dir || !id) return fail(MCB_ERR_INVALID, "NULL argument");
+  if (which < MCB_FIELD_PHI || which > MCB_FIELD_P)
+    return fail(MCB_ERR_INVALID, "unknown field %d", which);
+  if (step < 0) return fail(MCB_ERR_INVALID, "step must be >= 0");
+  const mcb::CaseDesc& d = h->s.cases[0];
+  std::vector<float> buf(static_cast<size_t>(d.ncell));
+  MCB_TRY(h->s.get_field(0, which, buf.data()));
+  return mcb_write_phi_file(dir, id, kNames[which], step, buf.data(), buf.size());
+}
+
 int mcb_write_info(const mcb_handle* h, const char* dir, const char* id,
                    const char* velocity_set, int save_every, int nsteps, double mlups) {
   if (!h || !dir || !id || !velocity_set) return fail(MCB_ERR_INVALID, "NULL argument");
@@ -940,7 +994,8 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   int rc = snapshot(false);
   double best = -1.0;
   int bv = save_variant, bz = s.zchunk;
-  const int zc_list[] = {4, 8, 16, 32, 64};
+  // Balanced ranges of 1..4 resident waves, then fixed chunks.
+  const int zc_list[] = {-1, -2, -3, -4, 8, 16, 32};
   for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;

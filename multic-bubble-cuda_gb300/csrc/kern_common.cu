@@ -15,6 +15,9 @@ cudaError_t launch_phi_bf16(int variant, int gmode, const StepArgs& a, cudaStrea
 cudaError_t launch_collide_f32(int variant, int gmode, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_collide_f16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t occupancy_f32(int variant, int gmode, int* phi_blocks, int* collide_blocks);
+cudaError_t occupancy_f16(int variant, int gmode, int* phi_blocks, int* collide_blocks);
+cudaError_t occupancy_bf16(int variant, int gmode, int* phi_blocks, int* collide_blocks);
 cudaError_t launch_init_f32(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_f16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_bf16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
@@ -195,6 +198,16 @@ cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& 
     case kStF32: return launch_collide_f32(variant, gmode, a, s);
     case kStF16: return launch_collide_f16(variant, gmode, a, s);
     case kStBF16: return launch_collide_bf16(variant, gmode, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t occupancy(int storage, int variant, int gmode, int* phi_blocks,
+                      int* collide_blocks) {
+  switch (storage) {
+    case kStF32: return occupancy_f32(variant, gmode, phi_blocks, collide_blocks);
+    case kStF16: return occupancy_f16(variant, gmode, phi_blocks, collide_blocks);
+    case kStBF16: return occupancy_bf16(variant, gmode, phi_blocks, collide_blocks);
     default: return cudaErrorInvalidValue;
   }
 }

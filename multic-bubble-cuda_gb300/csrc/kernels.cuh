@@ -192,38 +192,57 @@ __device__ __forceinline__ void prefetch_rows(int tid, const char* base, long lo
   }
 }
 
-__device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int tile) {
+// Last case whose first index (tile0 or plane0) is <= key.
+template <bool kPlanes>
+__device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int key) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&cs[mid].tile0) <= tile) lo = mid;
+    if ((kPlanes ? __ldg(&cs[mid].plane0) : __ldg(&cs[mid].tile0)) <= key) lo = mid;
     else hi = mid - 1;
   }
   return lo;
 }
 
 struct Tile {
-  int nx, ny, nz, bc, zb, ze, xt, yt;
+  int nx, ny, nz, bc, zb, ze, xt, yt, ci;
   long long ncell, cell_off, f_off, g_off;
 };
 
+// The tile-planes [p0, p1) of this block.
+__device__ __forceinline__ int2 block_range(const StepArgs& a) {
+  const int b = static_cast<int>(blockIdx.x);
+  if (a.balanced) {
+    const long long P = a.planes, G = gridDim.x;
+    return make_int2(static_cast<int>(b * P / G), static_cast<int>((b + 1) * P / G));
+  }
+  const CaseDesc* cd = a.cases + find_case<false>(a.cases, a.ncases, b);
+  const int cols = __ldg(&cd->tiles_x) * __ldg(&cd->tiles_y);
+  const int r = b - __ldg(&cd->tile0);
+  const int nz = __ldg(&cd->nz), zc = __ldg(&cd->zchunk);
+  const int base = __ldg(&cd->plane0) + (r % cols) * nz;
+  const int z0 = (r / cols) * zc;
+  return make_int2(base + z0, base + min(z0 + zc, nz));
+}
+
+// The column piece that starts at tile-plane p and ends at p1 or at the column's top.
 template <int BX, int BY>
-__device__ __forceinline__ Tile locate_tile(const StepArgs& a) {
-  const int c = find_case(a.cases, a.ncases, blockIdx.x);
+__device__ __forceinline__ Tile segment_tile(const StepArgs& a, int p, int p1) {
+  const int c = find_case<true>(a.cases, a.ncases, p);
   const CaseDesc* cd = a.cases + c;
   Tile t;
+  t.ci = c;
   t.nx = __ldg(&cd->nx);
   t.ny = __ldg(&cd->ny);
   t.nz = __ldg(&cd->nz);
   t.bc = __ldg(&cd->bc);
-  const int tiles_x = __ldg(&cd->tiles_x), tiles_y = __ldg(&cd->tiles_y);
-  const int zchunk = __ldg(&cd->zchunk);
-  int r = static_cast<int>(blockIdx.x) - __ldg(&cd->tile0);
-  t.xt = (r % tiles_x) * BX;
-  r /= tiles_x;
-  t.yt = (r % tiles_y) * BY;
-  t.zb = (r / tiles_y) * zchunk;
-  t.ze = min(t.zb + zchunk, t.nz);
+  const int tiles_x = __ldg(&cd->tiles_x);
+  const int r = p - __ldg(&cd->plane0);
+  const int col = r / t.nz;
+  t.zb = r - col * t.nz;
+  t.ze = min(t.nz, t.zb + (p1 - p));
+  t.xt = (col % tiles_x) * BX;
+  t.yt = (col / tiles_x) * BY;
   t.ncell = __ldg(&cd->ncell);
   t.cell_off = __ldg(&cd->cell_off);
   t.f_off = __ldg(&cd->f_off);
@@ -231,21 +250,32 @@ __device__ __forceinline__ Tile locate_tile(const StepArgs& a) {
   return t;
 }
 
+// Runs body(tile) over the column pieces of this block's range. sync: a block barrier
+// between pieces, for kernels whose pieces reuse shared memory.
+template <int BX, int BY, bool kSync, class Body>
+__device__ __forceinline__ void for_each_segment(const StepArgs& a, Body&& body) {
+  const int2 r = block_range(a);
+  for (int p = r.x; p < r.y;) {
+    const Tile t = segment_tile<BX, BY>(a, p, r.y);
+    if (kSync && p != r.x) __syncthreads();
+    body(t);
+    p += t.ze - t.zb;
+  }
+}
+
 // Register budgets, the largest warp counts per SM that compile without spills: 24 for
-// k_collide (80 registers); for k_phi, 40 with 32-bit storage (48 registers) and 32 with
-// the 16-bit decode (64 registers). Both kernels wait on loads, so resident warps hide
+// k_collide (80 registers); for k_phi, 32 with 32-bit storage (64 registers) and 24 with
+// the 16-bit decode (80 registers). Both kernels wait on loads, so resident warps hide
 // latency.
 constexpr int kCollideWarpsPerSM = 24;
 template <class S>
-constexpr int phi_warps_per_sm() { return S::kDev ? 32 : 40; }
+constexpr int phi_warps_per_sm() { return S::kDev ? 24 : 32; }
 
 // ---------------------------------------------------------------- k_phi: g -> phi --
 
 template <class S, int BX, int BY>
-__global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY))
-    k_phi(const StepArgs a) {
+__device__ __forceinline__ void phi_segment(const StepArgs& a, const Tile& t) {
   using GT = typename S::GT;
-  const Tile t = locate_tile<BX, BY>(a);
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int x = t.xt + static_cast<int>(threadIdx.x);
   const int y = t.yt + static_cast<int>(threadIdx.y);
@@ -313,6 +343,12 @@ __global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY
   }
 }
 
+template <class S, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY))
+    k_phi(const StepArgs a) {
+  for_each_segment<BX, BY, false>(a, [&](const Tile& t) { phi_segment<S, BX, BY>(a, t); });
+}
+
 // ------------------------------------- k_phi_eq: g -> phi when g is stored as (phi, J) --
 //
 // With full g relaxation, the post-collision population l of a cell is the equilibrium
@@ -347,8 +383,7 @@ __device__ __forceinline__ int q_rec(float4 r) {
 }
 
 template <class S, int BX, int BY>
-__global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const StepArgs a) {
-  const Tile t = locate_tile<BX, BY>(a);
+__device__ __forceinline__ void phi_eq_segment(const StepArgs& a, const Tile& t) {
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int x = t.xt + static_cast<int>(threadIdx.x);
   const int y = t.yt + static_cast<int>(threadIdx.y);
@@ -399,11 +434,15 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
   for (int z = t.zb; z < t.ze; ++z) pcur[x + yo + z * nxy] = cell(z);
 }
 
+template <class S, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const StepArgs a) {
+  for_each_segment<BX, BY, false>(a, [&](const Tile& t) { phi_eq_segment<S, BX, BY>(a, t); });
+}
+
 // ------------------------------------------------------- k_collide: the fused update --
 
 template <class S, int GM, int BX, int BY>
-__global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
-    k_collide(const StepArgs a) {
+__device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t) {
   constexpr bool BGK = GM == kGBgk;
   constexpr bool EQ = GM == kGEquil;
   using FT = typename S::FT;
@@ -415,7 +454,6 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   __shared__ float sphi[5][PP];
   __shared__ float snrm[3][4][HP];  // nx, ny, nz, |grad phi| of three planes
 
-  const Tile t = locate_tile<BX, BY>(a);
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int nxy = nx * ny;
   const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
@@ -424,7 +462,7 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   const bool active = x < nx && y < ny;
   const long long n = t.ncell;
 
-  const CaseDesc* cd = a.cases + find_case(a.cases, a.ncases, blockIdx.x);
+  const CaseDesc* cd = a.cases + t.ci;
   const float omega = __ldg(&cd->omega), omega_g = __ldg(&cd->omega_g);
   const float sigma = __ldg(&cd->sigma), sharp_c = __ldg(&cd->sharp_c);
   const float gravity = __ldg(&cd->gravity), phi_mean = __ldg(&cd->phi_mean);
@@ -747,6 +785,13 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
   }
 }
 
+template <class S, int GM, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
+    k_collide(const StepArgs a) {
+  for_each_segment<BX, BY, true>(a,
+                                 [&](const Tile& t) { collide_segment<S, GM, BX, BY>(a, t); });
+}
+
 // ------------------------------------------------------------------ k_init: fields --
 
 // Writes the stored populations so that the first update gathers the equilibria of the
@@ -841,38 +886,64 @@ __global__ void k_init(const InitArgs a) {
 
 // ------------------------------------------------------------------------ dispatch --
 
+// Kernel entry and block shape of each tile variant (kVariants order).
+template <class S, int BX, int BY>
+const void* phi_kernel_of(bool eq) {
+  return eq ? reinterpret_cast<const void*>(k_phi_eq<S, BX, BY>)
+            : reinterpret_cast<const void*>(k_phi<S, BX, BY>);
+}
+
 template <class S>
-cudaError_t phi_variant(int variant, bool eq, const StepArgs& a, cudaStream_t s) {
-  if (eq) {
-    switch (variant) {
-      case 0: k_phi_eq<S, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
-      case 1: k_phi_eq<S, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
-      case 2: k_phi_eq<S, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
-      case 3: k_phi_eq<S, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
-      default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
-  }
+const void* phi_kernel(int variant, bool eq, dim3* block) {
   switch (variant) {
-    case 0: k_phi<S, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
-    case 1: k_phi<S, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
-    case 2: k_phi<S, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
-    case 3: k_phi<S, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
-    default: return cudaErrorInvalidValue;
+    case 0: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
+    case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
+    case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
+    case 3: *block = dim3(16, 8); return phi_kernel_of<S, 16, 8>(eq);
+    default: return nullptr;
   }
-  return cudaGetLastError();
 }
 
 template <class S, int GM>
-cudaError_t collide_variant(int variant, const StepArgs& a, cudaStream_t s) {
+const void* collide_kernel(int variant, dim3* block) {
   switch (variant) {
-    case 0: k_collide<S, GM, 32, 8><<<a.ntiles, dim3(32, 8), 0, s>>>(a); break;
-    case 1: k_collide<S, GM, 16, 16><<<a.ntiles, dim3(16, 16), 0, s>>>(a); break;
-    case 2: k_collide<S, GM, 64, 4><<<a.ntiles, dim3(64, 4), 0, s>>>(a); break;
-    case 3: k_collide<S, GM, 16, 8><<<a.ntiles, dim3(16, 8), 0, s>>>(a); break;
-    default: return cudaErrorInvalidValue;
+    case 0: *block = dim3(32, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 32, 8>);
+    case 1: *block = dim3(16, 16); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 16>);
+    case 2: *block = dim3(64, 4); return reinterpret_cast<const void*>(k_collide<S, GM, 64, 4>);
+    case 3: *block = dim3(16, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 8>);
+    default: return nullptr;
   }
-  return cudaGetLastError();
+}
+
+template <class S>
+const void* collide_kernel_gm(int variant, int gmode, dim3* block) {
+  switch (gmode) {
+    case kGPop: return collide_kernel<S, kGPop>(variant, block);
+    case kGBgk: return collide_kernel<S, kGBgk>(variant, block);
+    case kGEquil: return collide_kernel<S, kGEquil>(variant, block);
+    default: return nullptr;
+  }
+}
+
+inline cudaError_t launch_on(const void* fn, int grid, dim3 block, const StepArgs& a,
+                             cudaStream_t s) {
+  if (!fn || grid <= 0) return cudaErrorInvalidValue;
+  void* args[] = {const_cast<StepArgs*>(&a)};
+  return cudaLaunchKernel(fn, dim3(grid), block, args, 0, s);
+}
+
+// Resident blocks per SM of the phi and collide kernels of a variant.
+template <class S>
+cudaError_t occupancy_of(int variant, int gmode, int* phi_blocks, int* collide_blocks) {
+  dim3 bp, bc;
+  const void* fp = phi_kernel<S>(variant, gmode == kGEquil, &bp);
+  const void* fc = collide_kernel_gm<S>(variant, gmode, &bc);
+  if (!fp || !fc) return cudaErrorInvalidValue;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(collide_blocks, fc,
+                                                       static_cast<int>(bc.x * bc.y), 0);
 }
 
 template <class S>
@@ -887,16 +958,19 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
 #define MCB_STORAGE_LAUNCHERS(S, suffix)                                                   \
   cudaError_t launch_phi_##suffix(int variant, int gmode, const StepArgs& a,               \
                                   cudaStream_t s) {                                        \
-    return phi_variant<S>(variant, gmode == kGEquil, a, s);                                \
+    dim3 block;                                                                            \
+    const void* fn = phi_kernel<S>(variant, gmode == kGEquil, &block);                     \
+    return launch_on(fn, a.grid_phi, block, a, s);                                         \
   }                                                                                        \
   cudaError_t launch_collide_##suffix(int variant, int gmode, const StepArgs& a,           \
                                       cudaStream_t s) {                                    \
-    switch (gmode) {                                                                       \
-      case kGPop: return collide_variant<S, kGPop>(variant, a, s);                         \
-      case kGBgk: return collide_variant<S, kGBgk>(variant, a, s);                         \
-      case kGEquil: return collide_variant<S, kGEquil>(variant, a, s);                     \
-      default: return cudaErrorInvalidValue;                                               \
-    }                                                                                      \
+    dim3 block;                                                                            \
+    const void* fn = collide_kernel_gm<S>(variant, gmode, &block);                         \
+    return launch_on(fn, a.grid_collide, block, a, s);                                     \
+  }                                                                                        \
+  cudaError_t occupancy_##suffix(int variant, int gmode, int* phi_blocks,                  \
+                                 int* collide_blocks) {                                    \
+    return occupancy_of<S>(variant, gmode, phi_blocks, collide_blocks);                    \
   }                                                                                        \
   cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
                                    cudaStream_t s) {                                       \

@@ -24,7 +24,7 @@ struct CaseDesc {
   int nx, ny, nz, bc;
   int tiles_x, tiles_y, tiles_z, zchunk;  // tile decomposition of this launch
   int tile0;                              // first tile (block) index of this case
-  int pad0;
+  int plane0;                             // first tile-plane index of this case
   long long ncell;     // nx*ny*nz
   long long cell_off;  // offset of the case's cells in per-cell arrays (phi, rest, macros)
   long long f_off;     // element offset of the case's 19*ncell f values
@@ -39,10 +39,21 @@ struct CaseDesc {
 
 // Buffers of one update. Populations are stored post-collision at the cell that
 // collided them ("pull" layout): an update gathers f*(x - c_l, l).
+// Work of a launch: tile-planes, one BX x BY tile of one z plane, numbered case by case,
+// column tile by column tile, z fastest. A block takes a contiguous range and marches each
+// column piece of it in z.
+//   - fixed chunks (balanced == 0): block b takes z chunk b of the tile table (tile0,
+//     tiles_x, tiles_y, tiles_z, zchunk); grid = ntiles.
+//   - balanced (balanced == 1): block b of G takes [b P / G, (b+1) P / G) of the P planes,
+//     so every block has the same work and G is a whole number of resident waves.
 struct StepArgs {
   const CaseDesc* cases;
   int ncases;
   int ntiles;
+  int balanced;
+  int planes;          // P, tile-planes of all cases
+  int grid_phi;        // blocks of the phi kernel
+  int grid_collide;    // blocks of the collide kernel
   const void* f_in;   // 19 arrays per case
   void* f_out;
   const void* g_in;   // 18 moving g arrays per case (l = 1..18)
@@ -103,6 +114,9 @@ cudaError_t launch_phi(int storage, int variant, int gmode, const StepArgs& a,
                        cudaStream_t s);
 cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& a,
                            cudaStream_t s);
+// Resident blocks per SM of the phi and collide kernels of a tile variant.
+cudaError_t occupancy(int storage, int variant, int gmode, int* phi_blocks,
+                      int* collide_blocks);
 cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);
 cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s);

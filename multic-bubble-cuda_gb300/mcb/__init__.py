@@ -36,7 +36,7 @@ EXPORTS = [
     "mcb_fill_phi_bubbles", "mcb_workload", "mcb_batch_create", "mcb_batch_destroy",
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
     "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
-    "mcb_checkpoint_save", "mcb_checkpoint_load",
+    "mcb_checkpoint_save", "mcb_checkpoint_load", "mcb_dump_field",
 ]
 
 
@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
             "mcb_write_info_file": [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int,
                                     C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_int, C.c_int, C.c_double],
+            "mcb_dump_field": [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int],
             "mcb_checkpoint_save": [vp, C.c_char_p],
             "mcb_checkpoint_load": [vp, C.c_char_p],
             "mcb_get_update": [vp, C.POINTER(C.c_int)],
@@ -280,6 +281,12 @@ class Solver:
 
     def dump_phi(self, directory: str, sim_id: str, step: int) -> None:
         _check(lib().mcb_dump_phi(self._h, directory.encode(), sim_id.encode(), step))
+
+    def dump_field(self, name: str, directory: str, sim_id: str, step: int) -> None:
+        """Writes <directory><sim_id>_<name>%06d.bin; name is a FIELDS key ("p" is
+        written as "pres")."""
+        _check(lib().mcb_dump_field(self._h, directory.encode(), sim_id.encode(),
+                                    FIELDS[name], step))
 
     def write_info(self, directory: str, sim_id: str, velocity_set: str = "D3Q19",
                    save_every: int = 100, nsteps: int = 0, mlups: float = 0.0) -> None:

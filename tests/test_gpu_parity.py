@@ -188,10 +188,24 @@ def test_tile_variants_graphs_and_chunks_agree_bitwise():
     base = gpu_run(cfg, phi, u, steps=41, variant=0, use_graph=0, zchunk=0)
     for v in range(mcb.lib().mcb_variant_count()):
         for g in (0, 1):
-            for zc in (0, 4, 7):
+            for zc in (0, -3, 4, 7):
                 r = gpu_run(cfg, phi, u, steps=41, variant=v, use_graph=g, zchunk=zc)
                 for k in FIELDS:
                     assert np.array_equal(r[k], base[k]), (v, g, zc, k)
+
+
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
+def test_work_splits_agree_bitwise_with_equilibrium_g(storage):
+    """Balanced ranges (pieces that start mid-column and span columns) and fixed chunks
+    give the same fields, bit for bit."""
+    cfg, phi, u = small_case(mcb.BC_WALLS_Z, n=(72, 40, 96), gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    base = gpu_run(cfg, phi, u, steps=23, variant=0, zchunk=5)
+    for v in range(mcb.lib().mcb_variant_count()):
+        for zc in (0, -1, -2, -7, 16):
+            r = gpu_run(cfg, phi, u, steps=23, variant=v, zchunk=zc)
+            for k in FIELDS:
+                assert np.array_equal(r[k], base[k]), (v, zc, k)
 
 
 def test_steps_split_across_calls_agree_bitwise():
@@ -283,6 +297,24 @@ def test_dump_files_hold_the_phi_field(tmp_path):
     assert "Precision: float" in text and "NZ_TOTAL: 28" in text
 
 
+def test_field_dumps_are_read_by_post_file_treat_names(tmp_path):
+    cfg, phi, u = small_case(mcb.BC_WALLS_Z, gravity=1e-4)
+    d = str(tmp_path) + "/"
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi)
+        s.step(3)
+        for name in ("phi", "rho", "ux", "uy", "uz", "p"):
+            s.dump_field(name, d, "002", 2)
+        want = {k: s.get(k) for k in ("phi", "rho", "ux", "uy", "uz", "p")}
+        with pytest.raises(mcb.McbError):
+            lib = mcb.lib()
+            mcb._check(lib.mcb_dump_field(s._h, d.encode(), b"002", 9, 2))
+    for name, fname in (("phi", "phi"), ("rho", "rho"), ("ux", "ux"), ("uy", "uy"),
+                        ("uz", "uz"), ("p", "pres")):
+        raw = np.fromfile(tmp_path / f"002_{fname}000002.bin", np.float32)
+        assert np.array_equal(raw.reshape(want[name].shape), want[name]), name
+
+
 def test_autotune_restores_the_state():
     cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(32, 32, 32), noise=1e-3)
     ref = gpu_run(cfg, phi, u, steps=20)
@@ -290,7 +322,8 @@ def test_autotune_restores_the_state():
         s.set_fields(phi, *u)
         s.step(10)
         v, zc, ml = s.autotune(nsteps=4)
-        assert 0 <= v < mcb.lib().mcb_variant_count() and zc > 0 and ml > 0
+        # zc > 0: fixed chunks; zc < 0: balanced over -zc waves.
+        assert 0 <= v < mcb.lib().mcb_variant_count() and -16 <= zc != 0 and ml > 0
         s.step(10)
         for k in FIELDS:
             assert np.array_equal(s.get(k).astype(np.float64), ref[k]), k

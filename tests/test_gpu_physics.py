@@ -133,3 +133,29 @@ def test_command_line_driver_writes_reference_style_output(tmp_path):
         assert a.size == n and np.all(np.isfinite(a)) and 0.3 < a.max() <= 1.1
     info = (tmp_path / "042_info.txt").read_text()
     assert "NX: 16" in info and "Precision: float" in info and "MLUPS:" in info
+
+
+def test_command_line_restart_continues_bitwise(tmp_path):
+    """A run stopped after update 10 with --checkpoint and resumed with --restart dumps the
+    same update-20 fields, bit for bit, as the uninterrupted run."""
+    import subprocess
+
+    exe = mcb.LIB_PATH.parent / "mcb_sim"
+    base = [str(exe), "D3Q19", "007", "--scenario", "2", "--scale", "0.125", "--save", "10",
+            "--fields", "phi,rho,uz,pres"]
+    ck = str(tmp_path / "s.ckpt")
+    runs = {"whole": ["--steps", "20"], "first": ["--steps", "10", "--checkpoint", ck],
+            "rest": ["--steps", "20", "--restart", ck]}
+    for name, extra in runs.items():
+        (tmp_path / name).mkdir()
+        r = subprocess.run(base + extra + ["--out", str(tmp_path / name) + "/"],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, (name, r.stdout + r.stderr)
+    rest = sorted(p.name for p in (tmp_path / "rest").iterdir())
+    assert rest == ["007_info.txt", "007_phi000020.bin", "007_pres000020.bin",
+                    "007_rho000020.bin", "007_uz000020.bin"]
+    for nm in rest[1:]:
+        assert (tmp_path / "rest" / nm).read_bytes() == (tmp_path / "whole" / nm).read_bytes()
+    rho = np.fromfile(tmp_path / "whole" / "007_rho000020.bin", np.float32)
+    pres = np.fromfile(tmp_path / "whole" / "007_pres000020.bin", np.float32)
+    np.testing.assert_allclose(pres, rho / 3, rtol=1e-6)

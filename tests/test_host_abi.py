@@ -41,7 +41,7 @@ def test_config_default_is_the_reference_case(built):
 @pytest.mark.parametrize("field,value,needle", [
     ("nx", 2, "below 4"), ("tau", 0.4, "tau must"), ("tau_g", 0.5, "tau_g must"),
     ("bc", 7, "boundary"), ("storage", 9, "storage"), ("width", 0.0, "width"),
-    ("variant", 99, "variant"), ("zchunk", -1, "zchunk")])
+    ("variant", 99, "variant"), ("zchunk", -17, "zchunk")])
 def test_invalid_configs_are_rejected_before_touching_the_gpu(built, field, value, needle):
     c = mcb.default_config(bc=mcb.BC_PERIODIC, tau_g=1.0)
     setattr(c, field, value)
@@ -129,6 +129,26 @@ def test_dump_and_info_round_trip_through_post_file_treat(built, tmp_path):
     for s, a in fields.items():
         got = ft.getMacrsFromStep(s, d)["phi"]  # (x, y, z) after fileTreat's swapaxes
         assert np.array_equal(got, np.swapaxes(a, 0, 2))
+
+
+def test_extra_field_dumps_are_told_apart_by_post_file_treat(built, tmp_path):
+    """With the dumped names added to __macr_names__ (post/fileTreat.py:8), the reader
+    matches each file to its field by substring; "pres" is not a substring of another
+    name, where "p" would be of "phi"."""
+    ft = _load_file_treat()
+    names = ["phi", "rho", "ux", "uy", "uz", "pres"]
+    nx, ny, nz = 4, 3, 5
+    d = str(tmp_path) + "/"
+    mcb.write_info_file(d, "009", "D3Q19", nx, ny, nz, 0.7, nsteps=10)
+    rng = np.random.default_rng(1)
+    data = {k: rng.random((nz, ny, nx), dtype=np.float32) for k in names}
+    for k, a in data.items():
+        mcb.write_phi_file(d, "009", k, 10, a)
+    ft.__macr_names__ = names
+    got = ft.getMacrsFromStep(10, d)
+    assert sorted(got) == sorted(names)
+    for k in names:
+        assert np.array_equal(got[k], np.swapaxes(data[k], 0, 2)), k
 
 
 def test_writers_report_io_errors(built, tmp_path):
