@@ -179,6 +179,10 @@ int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_s
                          int nx, int ny, int nz, double tau, double umax, double fx,
                          double fy, double fz, int save_every, int nsteps, double mlups);
 
+/* The tile variant and z chunk setting the handle runs (after defaults and autotuning).
+ * variant 4 is the TMA-staged 32x8 collide on the padded f layout. */
+int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
+
 /* Checkpoint and restart. No counterpart in the reference, which saves only phi
  * (src/main.cu:184-189) and so cannot resume. mcb_checkpoint_save writes everything the
  * next update reads:

@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap, cuTensorMapEncodeTiled (through the runtime entry point)
+
 #include "mcb.h"
 #include "lattice.h"
 #include "solver.h"
@@ -106,6 +108,9 @@ struct Solver {
   long long cells_total = 0, max_cells = 0;
   bool bgk = false;
   int gmode = mcb::kGPop;
+  bool padded = false;     // f in the padded layout of the TMA collide
+  CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
+  int* err = nullptr;      // device error flag of bounded waits
   mcb::CaseDesc* d_cases = nullptr;
   void* jbuf = nullptr;
   void* f[2] = {nullptr, nullptr};
@@ -153,6 +158,8 @@ struct Solver {
       rest[i] = p[i] = nullptr;
     }
     cudaFree(macros);
+    cudaFree(err);
+    err = nullptr;
     cudaFree(jbuf);
     jbuf = nullptr;
     cudaFree(stage);
@@ -281,15 +288,39 @@ struct Solver {
     bool force_pop = false;
     for (int i = 0; i < n; ++i) force_pop = force_pop || cs[i].g_mode == MCB_G_POPULATIONS;
     gmode = bgk ? mcb::kGBgk : (force_pop ? mcb::kGPop : mcb::kGEquil);
+    // The TMA collide, on request only (measured slower than the plain tiles on GB300):
+    // one case, (P, J) records, rows a multiple of 16 bytes. Elsewhere a request for it
+    // runs the plain 32x8 tile.
+    // Ghost columns: 32 bytes on each side keep every row's cells on 32-byte sectors.
+    const int gxe = 32 / static_cast<int>(pop_bytes(storage));
+    padded = n == 1 && gmode == mcb::kGEquil && cs[0].nx % (gxe / 2) == 0 &&
+             cs[0].variant == mcb::kTmaVariant && encode_fn() != nullptr;
+    if (padded) variant = mcb::kTmaVariant;
+    else if (variant == mcb::kTmaVariant) variant = 0;
+    for (auto& d : cases) {
+      if (padded) {
+        d.fgx = gxe;
+        d.fpx = d.nx + 2 * gxe;
+        d.fpy = d.ny + 2;
+        d.fn = static_cast<long long>(d.fpx) * d.fpy * d.nz;
+        d.f_off = 0;
+      } else {
+        d.fgx = 0;
+        d.fpx = d.nx;
+        d.fpy = d.ny;
+        d.fn = d.ncell;
+      }
+    }
     MCB_TRY(set_device());
     MCB_CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     MCB_CU(cudaEventCreate(&ev0));
     MCB_CU(cudaEventCreate(&ev1));
-    const size_t fb = static_cast<size_t>(cells_total) * 19 * pop_bytes(storage);
+    const size_t fb = f_bytes();
     const size_t gb = static_cast<size_t>(cells_total) * 18 * pop_bytes(storage);
     const size_t cb = static_cast<size_t>(cells_total) * sizeof(int);
     for (int i = 0; i < 2; ++i) {
       MCB_CU(cudaMalloc(&f[i], fb));
+      if (padded) MCB_CU(cudaMemset(f[i], 0, fb));  // ghost columns nothing reads stay 0
       if (gmode != mcb::kGEquil) {
         MCB_CU(cudaMalloc(&g[i], gb));
         MCB_CU(cudaMalloc(&rest[i], cb));
@@ -303,7 +334,68 @@ struct Solver {
     MCB_CU(cudaMalloc(&partials, sizeof(mcb::DiagPartial) * mcb::kDiagBlocks));
     MCB_CU(cudaMalloc(&result, sizeof(mcb::DiagPartial)));
     MCB_CU(cudaMalloc(&d_cases, sizeof(mcb::CaseDesc) * n));
+    MCB_CU(cudaMalloc(&err, sizeof(int)));
+    MCB_CU(cudaMemset(err, 0, sizeof(int)));
+    if (padded) {
+      MCB_CU(mcb::prepare_tma(storage));
+      for (int i = 0; i < 2; ++i) MCB_TRY(encode_fmap(i));
+    }
     return build_tiles();
+  }
+
+  size_t f_bytes() const {
+    const long long per = padded ? cases[0].fn : cells_total;
+    return static_cast<size_t>(per) * 19 * pop_bytes(storage);
+  }
+
+  // cuTensorMapEncodeTiled from the driver, through the runtime (no libcuda link).
+  using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                   CUtensorMapFloatOOBfill);
+  static EncodeTiled encode_fn() {
+    static EncodeTiled fn = [] {
+      void* p = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                           cudaEnableDefault, &q) != cudaSuccess ||
+          q != cudaDriverEntryPointSuccess)
+        p = nullptr;
+      return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+  }
+
+  // 4-D map of f[i]: (x, y, z, population) over the padded layout; box 32 + ghost width
+  // by 8 rows by 1 plane by 1 population. Out-of-range boxes read zeros.
+  int encode_fmap(int i) {
+    const mcb::CaseDesc& d = cases[0];
+    const size_t e = pop_bytes(storage);
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(d.fpx), static_cast<cuuint64_t>(d.fpy),
+                                static_cast<cuuint64_t>(d.nz), 19};
+    const cuuint64_t strides[3] = {d.fpx * e, static_cast<cuuint64_t>(d.fpx) * d.fpy * e,
+                                   static_cast<cuuint64_t>(d.fn) * e};
+    const cuuint32_t box[4] = {static_cast<cuuint32_t>(32 + d.fgx / 2), 8, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode_fn()(
+        &fmap[i], e == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+        f[i], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MCB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
+    return MCB_OK;
+  }
+
+  // Error flag of the kernels' bounded waits; read at every synchronisation point.
+  int check_err() {
+    int h = 0;
+    MCB_CU(cudaMemcpy(&h, err, sizeof h, cudaMemcpyDeviceToHost));
+    if (h != 0) {
+      cudaMemset(err, 0, sizeof(int));
+      return fail(MCB_ERR_CUDA, "a TMA wait in the collide kernel gave up (code %d)", h);
+    }
+    return MCB_OK;
   }
 
   int set_fields(int ci, const float* phi, const float* ux, const float* uy, const float* uz) {
@@ -372,6 +464,7 @@ struct Solver {
     a.planes = planes;
     a.grid_phi = grid_phi;
     a.grid_collide = grid_collide;
+    a.err = err;
     a.f_in = f[parity];
     a.f_out = f[parity ^ 1];
     a.g_in = g[parity];
@@ -394,7 +487,8 @@ struct Solver {
   int launch_update(bool with_macros) {
     const mcb::StepArgs a = args(with_macros);
     if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
-    MCB_CU(mcb::launch_collide(storage, variant, gmode, a, stream));
+    MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
+                               stream));
     latest_p = parity;
     parity ^= 1;
     first = 0;
@@ -477,7 +571,8 @@ struct Solver {
       const mcb::StepArgs a = args(i == nsteps - 1);
       if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 1], stream));
-      MCB_CU(mcb::launch_collide(storage, variant, gmode, a, stream));
+      MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
+                               stream));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 2], stream));
       latest_p = parity;
       parity ^= 1;
@@ -488,6 +583,7 @@ struct Solver {
     stepped = true;
     timed = true;
     MCB_CU(cudaEventSynchronize(ev1));
+    MCB_TRY(check_err());
     float tp = 0.f, tc = 0.f, tt = 0.f;
     for (int i = 0; i < nsteps; ++i) {
       float a = 0.f, b = 0.f;
@@ -515,7 +611,7 @@ struct Solver {
   std::vector<std::pair<void*, size_t>> ckpt_buffers() {
     const size_t n = static_cast<size_t>(cells_total);
     std::vector<std::pair<void*, size_t>> v;
-    v.push_back({f[parity], n * 19 * pop_bytes(storage)});
+    v.push_back({f[parity], f_bytes()});
     if (gmode == mcb::kGEquil) {
       v.push_back({jbuf, n * sizeof(float4)});
     } else {
@@ -547,6 +643,7 @@ struct Solver {
     hd.parity = parity;
     hd.first = first;
     hd.latest_p = latest_p;
+    hd.pad = padded ? cases[0].fgx : 0;  // f layout
     hd.update = update;
     hd.tau = cfg[0].tau;
     hd.tau_g = cfg[0].tau_g;
@@ -587,10 +684,11 @@ struct Solver {
     }
     mcb::CaseDesc& d = cases[0];
     if (hd.nx != d.nx || hd.ny != d.ny || hd.nz != d.nz || hd.bc != d.bc ||
-        hd.storage != storage || hd.gmode != gmode) {
+        hd.storage != storage || hd.gmode != gmode || hd.pad != (padded ? d.fgx : 0)) {
       std::fclose(fp);
       return fail(MCB_ERR_INVALID,
-                  "checkpoint %s was written for another size, boundary mode, storage or g mode",
+                  "checkpoint %s was written for another size, boundary mode, storage, g mode "
+                  "or f layout",
                   path);
     }
     MCB_CU(cudaStreamSynchronize(stream));
@@ -611,8 +709,7 @@ struct Solver {
     std::fclose(fp);
     if (!ok) return fail(MCB_ERR_IO, "%s is truncated", path);
     // Reference-mode shells keep f = W_l in both buffers: the other buffer takes the same.
-    const size_t fbytes = static_cast<size_t>(cells_total) * 19 * pop_bytes(storage);
-    MCB_CU(cudaMemcpy(f[parity ^ 1], f[parity], fbytes, cudaMemcpyDeviceToDevice));
+    MCB_CU(cudaMemcpy(f[parity ^ 1], f[parity], f_bytes(), cudaMemcpyDeviceToDevice));
     first = hd.first;
     latest_p = hd.latest_p;
     update = hd.update;
@@ -627,7 +724,7 @@ struct Solver {
   int sync() {
     MCB_TRY(set_device());
     MCB_CU(cudaStreamSynchronize(stream));
-    return MCB_OK;
+    return check_err();
   }
 
   int get_field(int ci, int which, float* host) {
@@ -644,6 +741,7 @@ struct Solver {
     MCB_CU(cudaMemcpyAsync(host, src, static_cast<size_t>(d.ncell) * sizeof(float),
                            cudaMemcpyDeviceToHost, stream));
     MCB_CU(cudaStreamSynchronize(stream));
+    MCB_TRY(check_err());
     const long long n = d.ncell;
     if (which == MCB_FIELD_P)
       for (long long i = 0; i < n; ++i) host[i] *= (1.0f / 3.0f);
@@ -684,6 +782,7 @@ struct Solver {
     mcb::DiagPartial r;
     MCB_CU(cudaMemcpyAsync(&r, result, sizeof r, cudaMemcpyDeviceToHost, stream));
     MCB_CU(cudaStreamSynchronize(stream));
+    MCB_TRY(check_err());
     std::memset(out, 0, sizeof *out);
     out->mass = r.mass;
     out->mass_q30 = r.mass_q30;
@@ -894,6 +993,13 @@ int mcb_checkpoint_load(mcb_handle* h, const char* path) {
   return h->s.ckpt_load(path);
 }
 
+int mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk) {
+  if (!h || !variant || !zchunk) return fail(MCB_ERR_INVALID, "NULL argument");
+  *variant = h->s.variant;
+  *zchunk = h->s.zchunk;
+  return MCB_OK;
+}
+
 int mcb_get_update(const mcb_handle* h, int* update) {
   if (!h || !update) return fail(MCB_ERR_INVALID, "NULL argument");
   *update = static_cast<int>(h->s.update);
@@ -940,7 +1046,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   const int par = s.parity;
   const size_t n = static_cast<size_t>(s.cells_total);
   const bool eq = s.gmode == mcb::kGEquil;
-  const size_t fb = n * 19 * pop_bytes(s.storage);
+  const size_t fb = s.f_bytes();
   // Equilibrium storage keeps a (phi, J) record per cell in place of g and its rest.
   const size_t gb = eq ? n * sizeof(float4) : n * 18 * pop_bytes(s.storage);
   void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
@@ -997,6 +1103,9 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   // Balanced ranges of 1..4 resident waves, then fixed chunks.
   const int zc_list[] = {-1, -2, -3, -4, 8, 16, 32};
   for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
+    // The f layout is fixed at creation: the TMA variant alone on the padded layout, the
+    // plain tiles otherwise.
+    if ((v == mcb::kTmaVariant) != s.padded) continue;
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;
       s.variant = v;

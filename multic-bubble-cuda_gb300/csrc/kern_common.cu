@@ -12,9 +12,18 @@ namespace mcb {
 cudaError_t launch_phi_f32(int variant, int gmode, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_phi_f16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_phi_bf16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_f32(int variant, int gmode, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_f16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_collide_f32(int variant, int gmode, const StepArgs& a, const void* tmap,
+                               cudaStream_t s);
+cudaError_t prepare_tma_f32();
+size_t tma_smem_f32();
+cudaError_t launch_collide_f16(int variant, int gmode, const StepArgs& a, const void* tmap,
+                               cudaStream_t s);
+cudaError_t prepare_tma_f16();
+size_t tma_smem_f16();
+cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, const void* tmap,
+                               cudaStream_t s);
+cudaError_t prepare_tma_bf16();
+size_t tma_smem_bf16();
 cudaError_t occupancy_f32(int variant, int gmode, int* phi_blocks, int* collide_blocks);
 cudaError_t occupancy_f16(int variant, int gmode, int* phi_blocks, int* collide_blocks);
 cudaError_t occupancy_bf16(int variant, int gmode, int* phi_blocks, int* collide_blocks);
@@ -193,12 +202,30 @@ cudaError_t launch_phi(int storage, int variant, int gmode, const StepArgs& a,
 }
 
 cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& a,
-                           cudaStream_t s) {
+                           const void* tmap_in, cudaStream_t s) {
   switch (storage) {
-    case kStF32: return launch_collide_f32(variant, gmode, a, s);
-    case kStF16: return launch_collide_f16(variant, gmode, a, s);
-    case kStBF16: return launch_collide_bf16(variant, gmode, a, s);
+    case kStF32: return launch_collide_f32(variant, gmode, a, tmap_in, s);
+    case kStF16: return launch_collide_f16(variant, gmode, a, tmap_in, s);
+    case kStBF16: return launch_collide_bf16(variant, gmode, a, tmap_in, s);
     default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t prepare_tma(int storage) {
+  switch (storage) {
+    case kStF32: return prepare_tma_f32();
+    case kStF16: return prepare_tma_f16();
+    case kStBF16: return prepare_tma_bf16();
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+size_t tma_smem_bytes(int storage) {
+  switch (storage) {
+    case kStF32: return tma_smem_f32();
+    case kStF16: return tma_smem_f16();
+    case kStBF16: return tma_smem_bf16();
+    default: return 0;
   }
 }
 

@@ -32,10 +32,12 @@
 // phi is invariant to the last bit in periodic and walled domains.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cfloat>
+#include <cstring>
 
 #include "lattice.h"
 #include "solver.h"
@@ -206,7 +208,8 @@ __device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int key) {
 
 struct Tile {
   int nx, ny, nz, bc, zb, ze, xt, yt, ci;
-  long long ncell, cell_off, f_off, g_off;
+  int fgx, fpx, fpy;
+  long long ncell, cell_off, f_off, g_off, fn;
 };
 
 // The tile-planes [p0, p1) of this block.
@@ -247,6 +250,10 @@ __device__ __forceinline__ Tile segment_tile(const StepArgs& a, int p, int p1) {
   t.cell_off = __ldg(&cd->cell_off);
   t.f_off = __ldg(&cd->f_off);
   t.g_off = __ldg(&cd->g_off);
+  t.fn = __ldg(&cd->fn);
+  t.fgx = __ldg(&cd->fgx);
+  t.fpx = __ldg(&cd->fpx);
+  t.fpy = __ldg(&cd->fpy);
   return t;
 }
 
@@ -439,10 +446,130 @@ __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const S
   for_each_segment<BX, BY, false>(a, [&](const Tile& t) { phi_eq_segment<S, BX, BY>(a, t); });
 }
 
+// ------------------------------------------- TMA staging of f for the collide kernel --
+//
+// The TMA variant loads, for every plane a block collides, the 19 pulled population boxes
+// of its 32x8 tile with cp.async.bulk.tensor (one instruction per box, issued by one
+// thread) into a two-stage shared-memory ring, completed on an mbarrier per stage. The
+// threads then read f_l(x - c_l) from shared memory at a fixed offset. Each box is the
+// tile widened by 16 bytes in x, so that its x origin stays 16-byte aligned whatever the
+// direction's x shift; periodic images come from the ghost columns (32 bytes a side) and
+// rows of the padded layout, which the collide kernel rewrites with every update.
+
+constexpr int kTmaBX = 32, kTmaBY = 8;
+constexpr int kTmaMaxSpin = 1 << 20;  // try_wait rounds before a wait gives up
+
+template <class FT>
+struct TmaBox {
+  static constexpr int kGX = 16 / static_cast<int>(sizeof(FT));  // x slop: 16 bytes
+  static constexpr int kW = kTmaBX + kGX;                         // box width (elements)
+  static constexpr int kBytes = kW * kTmaBY * static_cast<int>(sizeof(FT));
+  static_assert(kBytes % 128 == 0, "TMA boxes must keep 128-byte shared-memory alignment");
+  static constexpr int kStageBytes = kQ * kBytes;
+  static constexpr int kSmem = 2 * kStageBytes + 128;  // two stages + alignment slack
+};
+
+struct TmaPipe {
+  unsigned char* buf;        // 2 stages x 19 boxes
+  unsigned long long* mbar;  // one mbarrier per stage
+  const CUtensorMap* map;    // f_in
+  unsigned it;               // planes consumed by this block so far (stage = it & 1)
+  bool failed;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* m, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* m, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the given phase parity; false after kTmaMaxSpin rounds.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* m, unsigned parity) {
+  for (int i = 0; i < kTmaMaxSpin; ++i)
+    if (mbar_try_wait(m, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1,
+                                            int c2, int c3, unsigned long long* m) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+      "r"(smem_u32(m))
+      : "memory");
+}
+
+// Issues the 19 boxes that plane zt of a tile pulls into stage buffer dst (one thread).
+// Box l covers padded x [x0, x0 + kW), rows yt - cy .. yt - cy + 7, plane zt - cz (wrapped
+// when periodic; its own plane and population opp(l) across a z wall).
+template <class FT>
+__device__ __forceinline__ void tma_issue_plane(const TmaPipe& p, unsigned char* dst,
+                                                unsigned long long* m, int xt, int yt,
+                                                int zt, int nz, int bc, int gxl) {
+  constexpr int GX = TmaBox<FT>::kGX;
+  mbar_expect_tx(m, TmaBox<FT>::kStageBytes);
+  static_for<0, kQ>([&](auto LC) {
+    constexpr int L = decltype(LC)::value;
+    int zs = zt - cz(L), pop = L, y0 = yt + 1 - cy(L);
+    int x0 = gxl + xt - (cx(L) == 1 ? GX : 0);
+    if (cz(L) != 0 && (zs < 0 || zs >= nz)) {
+      if (bc == kBcWallsZ) {
+        zs = zt;
+        pop = opp(L);
+        x0 = gxl + xt;
+        y0 = yt + 1;
+      } else if (bc == kBcPeriodic) {
+        zs = zs < 0 ? zs + nz : zs - nz;
+      }  // reference mode: only shell planes reach past z; the box reads the fill value
+    }
+    tma_load_4d(dst + L * TmaBox<FT>::kBytes, p.map, x0, y0, zs, pop, m);
+  });
+}
+
+// Ghost copies of a freshly collided population of cell (x, y): the periodic images that
+// consumers across the x and y edges pull (padded layout, periodic x and y only).
+template <int L, class FT>
+__device__ __forceinline__ void f_ghosts(FT* f, long long fn, int x, int y, int z, int nx,
+                                         int ny, int gx, int px, int py, FT v) {
+  int gxp = -1, gyp = -1;
+  if (cx(L) == -1 && x == 0) gxp = nx + gx;
+  else if (cx(L) == 1 && x == nx - 1) gxp = gx - 1;
+  if (cy(L) == -1 && y == 0) gyp = ny + 1;
+  else if (cy(L) == 1 && y == ny - 1) gyp = 0;
+  if (gxp < 0 && gyp < 0) return;
+  FT* fl = f + L * fn + static_cast<long long>(z) * py * px;
+  if (gxp >= 0) fl[static_cast<long long>(y + 1) * px + gxp] = v;
+  if (gyp >= 0) fl[static_cast<long long>(gyp) * px + x + gx] = v;
+  if (gxp >= 0 && gyp >= 0) fl[static_cast<long long>(gyp) * px + gxp] = v;
+}
+
 // ------------------------------------------------------- k_collide: the fused update --
 
-template <class S, int GM, int BX, int BY>
-__device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t) {
+template <class S, int GM, int BX, int BY, bool kTma = false>
+__device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t,
+                                                TmaPipe* pipe = nullptr) {
   constexpr bool BGK = GM == kGBgk;
   constexpr bool EQ = GM == kGEquil;
   using FT = typename S::FT;
@@ -553,6 +680,23 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   float4* __restrict__ jout = EQ ? static_cast<float4*>(a.j) + t.cell_off : nullptr;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
+  // f layout of the stores: plain (fn = n, cell index) or padded (TMA variant).
+  const long long fn = kTma ? t.fn : n;
+  const bool ghosts = kTma && !ref;
+  using Box = TmaBox<FT>;
+  const unsigned it0 = kTma ? pipe->it : 0u;
+  if constexpr (kTma) {
+    // Planes zb and zb+1 into the two stages; each later plane is issued when the stage
+    // it reuses has been read.
+    if (tid == 0) {
+      for (int k = 0; k < 2 && t.zb + k < t.ze; ++k) {
+        const unsigned st = (it0 + k) & 1u;
+        tma_issue_plane<FT>(*pipe, pipe->buf + st * Box::kStageBytes, pipe->mbar + st, t.xt,
+                            t.yt, t.zb + k, nz, t.bc, t.fgx);
+      }
+    }
+  }
+
   // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
   for (int zpl = t.zb - 2; zpl <= t.zb + 1; ++zpl) {
     issue(zpl);
@@ -577,7 +721,41 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
 
     // Pull the 19 f populations (issued before the barriers to overlap their latency).
     FT fr[kQ];
-    if (work) {
+    if constexpr (kTma) {
+      const unsigned k = it0 + static_cast<unsigned>(z - t.zb);
+      const unsigned st = k & 1u;
+      const bool ok = mbar_wait_bounded(pipe->mbar + st, (k >> 1) & 1u);
+      if (work && ok) {
+        const FT* box = reinterpret_cast<const FT*>(pipe->buf + st * Box::kStageBytes);
+        static_for<0, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          // Column of x - c_l in the box of l (its origin is 16-byte aligned); across a
+          // z wall the box holds the cell's own column.
+          constexpr int RX = cx(L) == 1 ? Box::kGX - 1 : (cx(L) == -1 ? 1 : 0);
+          const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+          const int rx = (RX != 0 && bounce) ? 0 : RX;
+          fr[L] = box[L * (Box::kBytes / static_cast<int>(sizeof(FT))) + ty * Box::kW + tx + rx];
+        });
+      }
+      if (__syncthreads_or(!ok)) {
+        // A box never arrived: flag it, let the copies in flight land, leave the launch.
+        if (tid == 0) {
+          atomicExch(a.err, kErrTmaWait);
+          for (int q = 0; q < 2; ++q) {
+            const unsigned kk = k + q;
+            if (t.zb + static_cast<int>(kk - it0) < t.ze)
+              mbar_wait_bounded(pipe->mbar + (kk & 1u), (kk >> 1) & 1u);
+          }
+        }
+        __syncthreads();
+        pipe->failed = true;
+        return;
+      }
+      // Every thread has read stage st: refill it with plane z + 2.
+      if (tid == 0 && z + 2 < t.ze)
+        tma_issue_plane<FT>(*pipe, pipe->buf + st * Box::kStageBytes, pipe->mbar + st, t.xt,
+                            t.yt, z + 2, nz, t.bc, t.fgx);
+    } else if (work) {
       fr[0] = S::fload(fin + idx);
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
@@ -592,7 +770,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         }
       });
     }
-    __syncthreads();
+    if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
     normals(z + 1);
     __syncthreads();
     if (!active) continue;
@@ -729,10 +907,20 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       go[O] = W * (phi - dg);
     });
 
-    static_for<0, kQ>([&](auto LC) {
-      constexpr int L = decltype(LC)::value;
-      fout[L * n + idx] = S::template f_put<L>(fo[L]);
-    });
+    if constexpr (kTma) {
+      const long long pidx = (static_cast<long long>(z) * t.fpy + y + 1) * t.fpx + x + t.fgx;
+      static_for<0, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        const FT v = S::template f_put<L>(fo[L]);
+        fout[L * fn + pidx] = v;
+        if (ghosts) f_ghosts<L>(fout, fn, x, y, z, nx, ny, t.fgx, t.fpx, t.fpy, v);
+      });
+    } else {
+      static_for<0, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        fout[L * n + idx] = S::template f_put<L>(fo[L]);
+      });
+    }
 
     if constexpr (BGK) {
       // Incoming g (pull), decoded, then relaxed towards geq.
@@ -792,6 +980,28 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
                                  [&](const Tile& t) { collide_segment<S, GM, BX, BY>(a, t); });
 }
 
+// The TMA variant: 32x8 tiles, f staged through shared memory (one case, (P, J) records).
+template <class S>
+__global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kTmaBX * kTmaBY))
+    k_collide_tma(const StepArgs a, const __grid_constant__ CUtensorMap fmap) {
+  extern __shared__ __align__(1024) unsigned char tma_smem[];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // Boxes start on 128-byte boundaries of the shared window.
+  unsigned char* buf = tma_smem + ((128u - (smem_u32(tma_smem) & 127u)) & 127u);
+  TmaPipe pipe{buf, mbar, &fmap, 0u, false};
+  for_each_segment<kTmaBX, kTmaBY, true>(a, [&](const Tile& t) {
+    if (pipe.failed) return;
+    collide_segment<S, kGEquil, kTmaBX, kTmaBY, true>(a, t, &pipe);
+    pipe.it += static_cast<unsigned>(t.ze - t.zb);
+  });
+}
+
 // ------------------------------------------------------------------ k_init: fields --
 
 // Writes the stored populations so that the first update gathers the equilibria of the
@@ -834,6 +1044,11 @@ __global__ void k_init(const InitArgs a) {
   }
   FT* f0 = static_cast<FT*>(a.f0) + cd->f_off;
   FT* f1 = static_cast<FT*>(a.f1) + cd->f_off;
+  // f layout (plain: fidx = idx, fn = n; padded: ghost columns and rows, kept periodic).
+  const long long fn = cd->fn;
+  const long long fidx =
+      (static_cast<long long>(z) * cd->fpy + y + (cd->fgx ? 1 : 0)) * cd->fpx + x + cd->fgx;
+  const bool fghost = cd->fgx != 0 && !ref;
   GT* g0 = static_cast<GT*>(a.g0) + cd->g_off;
   static_for<0, kQ>([&](auto LC) {
     constexpr int L = decltype(LC)::value;
@@ -870,8 +1085,13 @@ __global__ void k_init(const InitArgs a) {
     float feq = wf(L) * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
     if (shell) feq = wf(L);
     const float fst = S::kFDev ? feq - wf(L) : feq;
-    f0[L * n + idx] = S::template f_put<L>(fst);
-    f1[L * n + idx] = S::template f_put<L>(fst);
+    const FT v = S::template f_put<L>(fst);
+    f0[L * fn + fidx] = v;
+    f1[L * fn + fidx] = v;
+    if (fghost) {
+      f_ghosts<L>(f0, fn, x, y, z, nx, ny, cd->fgx, cd->fpx, cd->fpy, v);
+      f_ghosts<L>(f1, fn, x, y, z, nx, ny, cd->fgx, cd->fpx, cd->fpy, v);
+    }
     if (eq) {
       // no g populations are stored
     } else if constexpr (L == 0) {
@@ -896,7 +1116,8 @@ const void* phi_kernel_of(bool eq) {
 template <class S>
 const void* phi_kernel(int variant, bool eq, dim3* block) {
   switch (variant) {
-    case 0: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
+    case 0:
+    case kTmaVariant: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
     case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
     case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
     case 3: *block = dim3(16, 8); return phi_kernel_of<S, 16, 8>(eq);
@@ -932,9 +1153,35 @@ inline cudaError_t launch_on(const void* fn, int grid, dim3 block, const StepArg
   return cudaLaunchKernel(fn, dim3(grid), block, args, 0, s);
 }
 
+template <class S>
+cudaError_t launch_collide_tma(const StepArgs& a, const void* tmap, cudaStream_t s) {
+  if (!tmap || a.grid_collide <= 0) return cudaErrorInvalidValue;
+  CUtensorMap map;
+  memcpy(&map, tmap, sizeof map);
+  k_collide_tma<S><<<a.grid_collide, dim3(kTmaBX, kTmaBY), TmaBox<typename S::FT>::kSmem, s>>>(
+      a, map);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t prepare_tma_kernel() {
+  return cudaFuncSetAttribute(k_collide_tma<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              TmaBox<typename S::FT>::kSmem);
+}
+
 // Resident blocks per SM of the phi and collide kernels of a variant.
 template <class S>
 cudaError_t occupancy_of(int variant, int gmode, int* phi_blocks, int* collide_blocks) {
+  if (variant == kTmaVariant) {
+    if (gmode != kGEquil) return cudaErrorInvalidValue;
+    dim3 bp;
+    const void* fp = phi_kernel<S>(0, true, &bp);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        collide_blocks, k_collide_tma<S>, kTmaBX * kTmaBY, TmaBox<typename S::FT>::kSmem);
+  }
   dim3 bp, bc;
   const void* fp = phi_kernel<S>(variant, gmode == kGEquil, &bp);
   const void* fc = collide_kernel_gm<S>(variant, gmode, &bc);
@@ -963,11 +1210,15 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
     return launch_on(fn, a.grid_phi, block, a, s);                                         \
   }                                                                                        \
   cudaError_t launch_collide_##suffix(int variant, int gmode, const StepArgs& a,           \
-                                      cudaStream_t s) {                                    \
+                                      const void* tmap, cudaStream_t s) {                  \
+    if (variant == kTmaVariant)                                                            \
+      return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
     dim3 block;                                                                            \
     const void* fn = collide_kernel_gm<S>(variant, gmode, &block);                         \
     return launch_on(fn, a.grid_collide, block, a, s);                                     \
   }                                                                                        \
+  cudaError_t prepare_tma_##suffix() { return prepare_tma_kernel<S>(); }                   \
+  size_t tma_smem_##suffix() { return TmaBox<typename S::FT>::kSmem; }                     \
   cudaError_t occupancy_##suffix(int variant, int gmode, int* phi_blocks,                  \
                                  int* collide_blocks) {                                    \
     return occupancy_of<S>(variant, gmode, phi_blocks, collide_blocks);                    \

@@ -29,6 +29,12 @@ struct CaseDesc {
   long long cell_off;  // offset of the case's cells in per-cell arrays (phi, rest, macros)
   long long f_off;     // element offset of the case's 19*ncell f values
   long long g_off;     // element offset of the case's 18*ncell moving g values
+  // f layout: element (l, x, y, z) at f_off + l*fn + (z*fpy + y + (fgx ? 1 : 0))*fpx + x + fgx.
+  // Plain: fgx 0, fpx nx, fpy ny, fn ncell. Padded (the TMA update): fgx ghost columns
+  // (16 bytes) on each side of a row and one ghost row on each side of a plane, which hold
+  // the periodic images of the opposite edge.
+  long long fn;
+  int fgx, fpx, fpy, pad1;
   float omega;         // 1/tau
   float omega_g;       // 1/tau_g
   float sigma;
@@ -54,6 +60,7 @@ struct StepArgs {
   int planes;          // P, tile-planes of all cases
   int grid_phi;        // blocks of the phi kernel
   int grid_collide;    // blocks of the collide kernel
+  int* err;            // set to a nonzero code when a bounded wait of a kernel gives up
   const void* f_in;   // 19 arrays per case
   void* f_out;
   const void* g_in;   // 18 moving g arrays per case (l = 1..18)
@@ -103,17 +110,27 @@ struct DiagArgs {
   DiagPartial* result;    // one entry
 };
 
-constexpr int kNumVariants = 4;
+constexpr int kNumVariants = 5;
 struct Variant { int bx, by; };
-constexpr Variant kVariants[kNumVariants] = {{32, 8}, {16, 16}, {64, 4}, {16, 8}};
+// Variant 4 is the 32x8 collide that stages f through the tensor memory accelerator (TMA)
+// on the padded f layout; it needs one case, (phi, J) records and nx a multiple of 16 bytes.
+constexpr Variant kVariants[kNumVariants] = {{32, 8}, {16, 16}, {64, 4}, {16, 8}, {32, 8}};
+constexpr int kTmaVariant = 4;
+constexpr int kErrTmaWait = 1;  // StepArgs::err: a TMA wait timed out
 constexpr int kDiagBlocks = 304;   // fixed grid: the reduction order never changes
 constexpr int kDiagThreads = 256;
 
 // Kernel launchers (kernels.cu). Each returns the launch status.
 cudaError_t launch_phi(int storage, int variant, int gmode, const StepArgs& a,
                        cudaStream_t s);
+// tmap_in: the CUtensorMap of f_in for the TMA variant (nullptr otherwise).
 cudaError_t launch_collide(int storage, int variant, int gmode, const StepArgs& a,
-                           cudaStream_t s);
+                           const void* tmap_in, cudaStream_t s);
+// Raises the dynamic shared memory limit of the TMA collide kernels (call once per device
+// before the first launch or occupancy query).
+cudaError_t prepare_tma(int storage);
+// Dynamic shared memory of the TMA collide kernel for a storage.
+size_t tma_smem_bytes(int storage);
 // Resident blocks per SM of the phi and collide kernels of a tile variant.
 cudaError_t occupancy(int storage, int variant, int gmode, int* phi_blocks,
                       int* collide_blocks);

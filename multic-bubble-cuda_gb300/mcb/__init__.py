@@ -36,7 +36,7 @@ EXPORTS = [
     "mcb_fill_phi_bubbles", "mcb_workload", "mcb_batch_create", "mcb_batch_destroy",
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
     "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
-    "mcb_checkpoint_save", "mcb_checkpoint_load", "mcb_dump_field",
+    "mcb_checkpoint_save", "mcb_checkpoint_load", "mcb_dump_field", "mcb_get_schedule",
 ]
 
 
@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
                                     C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     C.c_double, C.c_int, C.c_int, C.c_double],
             "mcb_dump_field": [vp, C.c_char_p, C.c_char_p, C.c_int, C.c_int],
+            "mcb_get_schedule": [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)],
             "mcb_checkpoint_save": [vp, C.c_char_p],
             "mcb_checkpoint_load": [vp, C.c_char_p],
             "mcb_get_update": [vp, C.POINTER(C.c_int)],
@@ -292,6 +293,13 @@ class Solver:
                    save_every: int = 100, nsteps: int = 0, mlups: float = 0.0) -> None:
         _check(lib().mcb_write_info(self._h, directory.encode(), sim_id.encode(),
                                     velocity_set.encode(), save_every, nsteps, mlups))
+
+    @property
+    def schedule(self) -> tuple[int, int]:
+        """(tile variant, z chunk setting) the handle runs; variant 4 is the TMA collide."""
+        v, z = C.c_int(), C.c_int()
+        _check(lib().mcb_get_schedule(self._h, C.byref(v), C.byref(z)))
+        return v.value, z.value
 
     def checkpoint_save(self, path: str) -> None:
         _check(lib().mcb_checkpoint_save(self._h, str(path).encode()))

@@ -194,6 +194,48 @@ def test_tile_variants_graphs_and_chunks_agree_bitwise():
                     assert np.array_equal(r[k], base[k]), (v, g, zc, k)
 
 
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
+@pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z, mcb.BC_REF])
+def test_tma_collide_matches_the_plain_tile_bitwise(bc, storage):
+    """The TMA-staged collide (padded f layout with periodic ghost columns and rows) gives
+    the fields of the plain 32x8 tile, bit for bit: partial tiles in x and y, walls,
+    periodic images, reference shells."""
+    if bc == mcb.BC_REF:
+        cfg, u = reference_cfg(32), None
+        cfg.nx, cfg.ny, cfg.nz = 48, 40, 36
+        phi = mcb.fill_phi_bubbles(48, 40, 36, bc, 4.0, [(20.3, 18.6, 17.1, 8.0)])
+    else:
+        cfg, phi, u = small_case(bc, n=(48, 20, 30), gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    runs = {}
+    for v in (4, 0):
+        cfg.variant = v
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, *(u if u is not None else (None, None, None)))
+            runs[v] = s.schedule[0]
+            s.step(37)
+            runs[(v, "f")] = {k: s.get(k) for k in FIELDS}
+    assert runs[4] == 4 and runs[0] == 0
+    for k in FIELDS:
+        assert np.array_equal(runs[(4, "f")][k], runs[(0, "f")][k]), k
+
+
+def test_tma_collide_is_skipped_where_it_does_not_apply():
+    # rows not a multiple of 16 bytes, stored g populations: the plain 32x8 tile runs
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(42, 20, 30))
+    cfg.variant = 4
+    with mcb.Solver(cfg) as s:
+        assert s.schedule[0] == 0
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30), tau_g=0.8)
+    cfg.variant = 4
+    with mcb.Solver(cfg) as s:
+        assert s.schedule[0] == 0
+    # the default is the plain tile
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30))
+    with mcb.Solver(cfg) as s:
+        assert s.schedule[0] == 0
+
+
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
 def test_work_splits_agree_bitwise_with_equilibrium_g(storage):
     """Balanced ranges (pieces that start mid-column and span columns) and fixed chunks
