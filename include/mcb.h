@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MCB_ABI_VERSION 2
+#define MCB_ABI_VERSION 3
 
 /* status codes */
 #define MCB_OK            0
@@ -92,6 +92,11 @@ typedef struct mcb_config {
                              update rebuilds the populations; with tau_g != 1 all 19 are
                              stored;
                            MCB_G_POPULATIONS: always store the 19 populations. */
+    int   velocity_set; /* velocity set of f: 19 (D3Q19, the reference's build) or 27
+                           (D3Q27 with the tables of src/var.cu:33-35,47-52; the
+                           reference's D3Q27 moments are unfinished, src/lbm.cu:174-218).
+                           g and the phi stencils are D3Q19 either way. D3Q27 runs the
+                           32x8 tile. */
 } mcb_config;
 
 #define MCB_G_AUTO         0

@@ -1,6 +1,6 @@
 // mcb_sim: command-line driver that replaces the reference's src/main.cu.
 //
-//   mcb_sim <velocity_set> <id> [options]
+//   mcb_sim <velocity_set> <id> [options]      velocity_set: D3Q19 or D3Q27 (for f)
 //
 // With no options it runs the reference's hard-coded case (src/var.cu:3-25,
 // src/init.cu:27-49, src/main.cu:35):
@@ -64,8 +64,8 @@ int main(int argc, char** argv) {
     return 1;
   }
   const std::string vs = argv[1], id = argv[2];
-  if (vs != "D3Q19") {
-    std::fprintf(stderr, "mcb_sim: only the D3Q19 velocity set is supported\n");
+  if (vs != "D3Q19" && vs != "D3Q27") {
+    std::fprintf(stderr, "mcb_sim: velocity set must be D3Q19 or D3Q27 (f; g is D3Q19)\n");
     return 1;
   }
   int nsteps = 25000, save = 100, scenario = -1, autotune = 0;
@@ -158,6 +158,7 @@ int main(int argc, char** argv) {
     if (rc) return die("mcb_workload", rc);
   }
   if (storage >= 0) cfg.storage = storage;
+  cfg.velocity_set = vs == "D3Q27" ? 27 : 19;
 
   mcb_handle* h = nullptr;
   if ((rc = mcb_create(&cfg, &h))) return die("mcb_create", rc);

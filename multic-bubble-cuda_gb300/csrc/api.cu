@@ -87,6 +87,9 @@ int validate(const mcb_config& c, int index) {
     return fail(MCB_ERR_INVALID, "case %d: non-finite parameter", index);
   if (c.variant < -1 || c.variant >= mcb::kNumVariants)
     return fail(MCB_ERR_INVALID, "case %d: variant %d out of range", index, c.variant);
+  if (c.velocity_set != 19 && c.velocity_set != 27)
+    return fail(MCB_ERR_INVALID, "case %d: velocity_set must be 19 or 27 (got %d)", index,
+                c.velocity_set);
   if (c.zchunk < -kMaxWaves)
     return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= -%d", index, kMaxWaves);
   if (c.g_mode != MCB_G_AUTO && c.g_mode != MCB_G_POPULATIONS)
@@ -108,6 +111,7 @@ struct Solver {
   long long cells_total = 0, max_cells = 0;
   bool bgk = false;
   int gmode = mcb::kGPop;
+  int qf = 19;             // velocity set of f
   bool padded = false;     // f in the padded layout of the TMA collide
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
@@ -228,7 +232,7 @@ struct Solver {
       const int waves = -zchunk;
       int nsm = 0, occ_phi = 0, occ_col = 0;
       MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-      MCB_CU(mcb::occupancy(storage, variant, gmode, &occ_phi, &occ_col));
+      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, &occ_phi, &occ_col));
       if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
         return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
       grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
@@ -251,9 +255,11 @@ struct Solver {
     for (int i = 0; i < n; ++i) MCB_TRY(validate(cs[i], i));
     storage = cs[0].storage;
     device = cs[0].device;
+    qf = cs[0].velocity_set;
     for (int i = 1; i < n; ++i)
-      if (cs[i].storage != storage || cs[i].device != device)
-        return fail(MCB_ERR_INVALID, "all cases of a batch must share storage and device");
+      if (cs[i].storage != storage || cs[i].device != device || cs[i].velocity_set != qf)
+        return fail(MCB_ERR_INVALID,
+                    "all cases of a batch must share storage, device and velocity set");
     // Default tile from measured sweeps on GB300: 32x8 (either storage).
     variant = cs[0].variant >= 0 ? cs[0].variant : 0;
     zchunk_req = cs[0].zchunk;
@@ -271,7 +277,7 @@ struct Solver {
       d.bc = c.bc;
       d.ncell = static_cast<long long>(c.nx) * c.ny * c.nz;
       d.cell_off = off;
-      d.f_off = off * 19;
+      d.f_off = off * qf;
       d.g_off = off * 18;
       d.omega = 1.0f / c.tau;
       d.omega_g = 1.0f / c.tau_g;
@@ -293,10 +299,10 @@ struct Solver {
     // runs the plain 32x8 tile.
     // Ghost columns: 32 bytes on each side keep every row's cells on 32-byte sectors.
     const int gxe = 32 / static_cast<int>(pop_bytes(storage));
-    padded = n == 1 && gmode == mcb::kGEquil && cs[0].nx % (gxe / 2) == 0 &&
+    padded = n == 1 && qf == 19 && gmode == mcb::kGEquil && cs[0].nx % (gxe / 2) == 0 &&
              cs[0].variant == mcb::kTmaVariant && encode_fn() != nullptr;
     if (padded) variant = mcb::kTmaVariant;
-    else if (variant == mcb::kTmaVariant) variant = 0;
+    else if (variant == mcb::kTmaVariant || qf == 27) variant = 0;  // D3Q27: the 32x8 tile
     for (auto& d : cases) {
       if (padded) {
         d.fgx = gxe;
@@ -345,7 +351,7 @@ struct Solver {
 
   size_t f_bytes() const {
     const long long per = padded ? cases[0].fn : cells_total;
-    return static_cast<size_t>(per) * 19 * pop_bytes(storage);
+    return static_cast<size_t>(per) * qf * pop_bytes(storage);
   }
 
   // cuTensorMapEncodeTiled from the driver, through the runtime (no libcuda link).
@@ -449,6 +455,7 @@ struct Solver {
     a.macros = macros;
     a.cells_total = cells_total;
     a.gmode = gmode;
+    a.qf = qf;
     MCB_CU(mcb::launch_init(storage, a, d.nx, d.ny, d.nz, stream));
     MCB_CU(cudaStreamSynchronize(stream));
     fields_set[ci] = 1;
@@ -465,6 +472,7 @@ struct Solver {
     a.grid_phi = grid_phi;
     a.grid_collide = grid_collide;
     a.err = err;
+    a.qf = qf;
     a.f_in = f[parity];
     a.f_out = f[parity ^ 1];
     a.g_in = g[parity];
@@ -602,7 +610,7 @@ struct Solver {
   // ---- checkpoint: header + raw device buffers ----
   struct CkptHeader {
     char magic[8];
-    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad;
+    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad, qf;
     long long update;
     float tau, tau_g, sigma, sharp_c, gravity, phi_mean;
   };
@@ -644,6 +652,7 @@ struct Solver {
     hd.first = first;
     hd.latest_p = latest_p;
     hd.pad = padded ? cases[0].fgx : 0;  // f layout
+    hd.qf = qf;
     hd.update = update;
     hd.tau = cfg[0].tau;
     hd.tau_g = cfg[0].tau_g;
@@ -684,11 +693,12 @@ struct Solver {
     }
     mcb::CaseDesc& d = cases[0];
     if (hd.nx != d.nx || hd.ny != d.ny || hd.nz != d.nz || hd.bc != d.bc ||
-        hd.storage != storage || hd.gmode != gmode || hd.pad != (padded ? d.fgx : 0)) {
+        hd.storage != storage || hd.gmode != gmode || hd.pad != (padded ? d.fgx : 0) ||
+        hd.qf != qf) {
       std::fclose(fp);
       return fail(MCB_ERR_INVALID,
-                  "checkpoint %s was written for another size, boundary mode, storage, g mode "
-                  "or f layout",
+                  "checkpoint %s was written for another size, boundary mode, storage, g mode, "
+                  "f layout or velocity set",
                   path);
     }
     MCB_CU(cudaStreamSynchronize(stream));
@@ -850,6 +860,7 @@ int mcb_config_default(mcb_config* c) {
   c->zchunk = 0;
   c->use_graph = 1;
   c->g_mode = MCB_G_AUTO;
+  c->velocity_set = 19;
   return MCB_OK;
 }
 
@@ -1106,6 +1117,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     // The f layout is fixed at creation: the TMA variant alone on the padded layout, the
     // plain tiles otherwise.
     if ((v == mcb::kTmaVariant) != s.padded) continue;
+    if (s.qf == 27 && v != 0) continue;  // D3Q27 runs the 32x8 tile
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;
       s.variant = v;

@@ -567,9 +567,11 @@ __device__ __forceinline__ void f_ghosts(FT* f, long long fn, int x, int y, int 
 
 // ------------------------------------------------------- k_collide: the fused update --
 
-template <class S, int GM, int BX, int BY, bool kTma = false>
+// QF: velocity set of f (19 or 27); g and the phi stencils are D3Q19 either way.
+template <class S, int GM, int BX, int BY, bool kTma = false, int QF = kQ>
 __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t,
                                                 TmaPipe* pipe = nullptr) {
+  static_assert(QF == kQ || !kTma, "the TMA collide is D3Q19");
   constexpr bool BGK = GM == kGBgk;
   constexpr bool EQ = GM == kGEquil;
   using FT = typename S::FT;
@@ -720,7 +722,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
 
     // Pull the 19 f populations (issued before the barriers to overlap their latency).
-    FT fr[kQ];
+    FT fr[QF];
     if constexpr (kTma) {
       const unsigned k = it0 + static_cast<unsigned>(z - t.zb);
       const unsigned st = k & 1u;
@@ -757,7 +759,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
                             t.yt, z + 2, nz, t.bc, t.fgx);
     } else if (work) {
       fr[0] = S::fload(fin + idx);
-      static_for<1, kQ>([&](auto LC) {
+      static_for<1, QF>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
         constexpr int O = opp(L);
         const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
@@ -830,18 +832,18 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     // and forcing parts reduce in closed form:
     //   sum c_a c_b feq = rho (cs^2 d_ab + u_a u_b)
     //   sum c_a c_b HeF = (u_a F_b + u_b F_a)/2 - 3/2 (u.F) u_a u_b
-    // This uses the 4th-order isotropy of D3Q19.
+    // This uses the 4th-order isotropy of D3Q19 and D3Q27.
     // 16-bit storage holds f_l - W_l: its moments start from those of the weights
     // (sum W = 1, sum W c_a c_b = d_ab / 3, odd moments 0).
-    float f[kQ];
-    static_for<0, kQ>([&](auto LC) {
+    float f[QF];
+    static_for<0, QF>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
       f[L] = S::template f_raw<L>(fr[L]);
     });
     constexpr float m0 = S::kFDev ? 1.0f : 0.0f, m2 = S::kFDev ? 1.0f / 3.0f : 0.0f;
     float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
     float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
-    static_for<0, kQ>([&](auto LC) {
+    static_for<0, QF>([&](auto LC) {
       constexpr int L = decltype(LC)::value;
       const float v = f[L];
       rho += v;
@@ -883,13 +885,13 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     const float A = sharp_c * phi * (1.0f - phi);
     const float phi3 = 3.0f * phi;
 
-    float fo[kQ];
+    float fo[QF];
     float go[kQ];
-    fo[0] = wf(0) * (base * R - om * tr3 + fshift);
-    static_for<0, 9>([&](auto KC) {
+    fo[0] = wfq<QF>(0) * (base * R - om * tr3 + fshift);
+    static_for<0, (QF - 1) / 2>([&](auto KC) {
       constexpr int L = 2 * decltype(KC)::value + 1;
       constexpr int O = L + 1;
-      constexpr float W = wf(L);
+      constexpr float W = wfq<QF>(L);
       float cu = 0.f, cF = 0.f, cn = 0.f, qp = -tr3;
       if constexpr (cx(L) != 0) { cu += cx(L) * ux; cF += cx(L) * Fx; cn += cx(L) * nc.x; qp += pxx; }
       if constexpr (cy(L) != 0) { cu += cy(L) * uy; cF += cy(L) * Fy; cn += cy(L) * nc.y; qp += pyy; }
@@ -902,9 +904,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       const float rf = 1.5f * cF;
       fo[L] = W * ((e0 + e1) * (R + rf) + q);
       fo[O] = W * ((e0 - e1) * (R - rf) + q);
-      const float dg = phi3 * cu + A * cn;
-      go[L] = W * (phi + dg);
-      go[O] = W * (phi - dg);
+      if constexpr (L < kQ) {
+        constexpr float WG = wf(L);  // g is D3Q19
+        const float dg = phi3 * cu + A * cn;
+        go[L] = WG * (phi + dg);
+        go[O] = WG * (phi - dg);
+      }
     });
 
     if constexpr (kTma) {
@@ -916,7 +921,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         if (ghosts) f_ghosts<L>(fout, fn, x, y, z, nx, ny, t.fgx, t.fpx, t.fpy, v);
       });
     } else {
-      static_for<0, kQ>([&](auto LC) {
+      static_for<0, QF>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
         fout[L * n + idx] = S::template f_put<L>(fo[L]);
       });
@@ -1002,6 +1007,13 @@ __global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kT
   });
 }
 
+// D3Q27 f: 32x8 tiles, two blocks of eight warps per SM (27 populations in flight).
+template <class S, int GM>
+__global__ void __launch_bounds__(256, 2) k_collide27(const StepArgs a) {
+  for_each_segment<32, 8, true>(
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27>(a, t); });
+}
+
 // ------------------------------------------------------------------ k_init: fields --
 
 // Writes the stored populations so that the first update gathers the equilibria of the
@@ -1009,7 +1021,7 @@ __global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kT
 // In pull layout the value stored at y for direction l is the one its consumer y + c_l
 // reads; with bounce-back the consumer is y itself, as direction opp(l).
 // (initDist, src/init.cu:51-80.)
-template <class S>
+template <class S, int QF>
 __global__ void k_init(const InitArgs a) {
   using FT = typename S::FT;
   using GT = typename S::GT;
@@ -1050,7 +1062,7 @@ __global__ void k_init(const InitArgs a) {
       (static_cast<long long>(z) * cd->fpy + y + (cd->fgx ? 1 : 0)) * cd->fpx + x + cd->fgx;
   const bool fghost = cd->fgx != 0 && !ref;
   GT* g0 = static_cast<GT*>(a.g0) + cd->g_off;
-  static_for<0, kQ>([&](auto LC) {
+  static_for<0, QF>([&](auto LC) {
     constexpr int L = decltype(LC)::value;
     int xc = x + cx(L), yc = y + cy(L), zc = z + cz(L);
     bool bounce = false;
@@ -1082,9 +1094,10 @@ __global__ void k_init(const InitArgs a) {
     const float sz = bounce ? -cz(L) : cz(L);
     const float cu = sx * ux + sy * uy + sz * uz;
     const float u2 = ux * ux + uy * uy + uz * uz;
-    float feq = wf(L) * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
-    if (shell) feq = wf(L);
-    const float fst = S::kFDev ? feq - wf(L) : feq;
+    constexpr float W = wfq<QF>(L);
+    float feq = W * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
+    if (shell) feq = W;
+    const float fst = S::kFDev ? feq - W : feq;
     const FT v = S::template f_put<L>(fst);
     f0[L * fn + fidx] = v;
     f1[L * fn + fidx] = v;
@@ -1096,7 +1109,7 @@ __global__ void k_init(const InitArgs a) {
       // no g populations are stored
     } else if constexpr (L == 0) {
       a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
-    } else {
+    } else if constexpr (L < kQ) {  // g is D3Q19
       const float geq = wf(L) * a.phi[ci] * (1.0f + 3.0f * cu);
       int q;
       g0[(L - 1) * n + idx] = S::template g_put<L>(geq, S::g_split(P), q);
@@ -1137,6 +1150,16 @@ const void* collide_kernel(int variant, dim3* block) {
 }
 
 template <class S>
+const void* collide27_kernel(int gmode) {
+  switch (gmode) {
+    case kGPop: return reinterpret_cast<const void*>(k_collide27<S, kGPop>);
+    case kGBgk: return reinterpret_cast<const void*>(k_collide27<S, kGBgk>);
+    case kGEquil: return reinterpret_cast<const void*>(k_collide27<S, kGEquil>);
+    default: return nullptr;
+  }
+}
+
+template <class S>
 const void* collide_kernel_gm(int variant, int gmode, dim3* block) {
   switch (gmode) {
     case kGPop: return collide_kernel<S, kGPop>(variant, block);
@@ -1171,7 +1194,16 @@ cudaError_t prepare_tma_kernel() {
 
 // Resident blocks per SM of the phi and collide kernels of a variant.
 template <class S>
-cudaError_t occupancy_of(int variant, int gmode, int* phi_blocks, int* collide_blocks) {
+cudaError_t occupancy_of(int variant, int gmode, int qf, int* phi_blocks, int* collide_blocks) {
+  if (qf == kQ27) {
+    dim3 bp;
+    const void* fp = phi_kernel<S>(0, gmode == kGEquil, &bp);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(collide_blocks,
+                                                         collide27_kernel<S>(gmode), 256, 0);
+  }
   if (variant == kTmaVariant) {
     if (gmode != kGEquil) return cudaErrorInvalidValue;
     dim3 bp;
@@ -1197,7 +1229,8 @@ template <class S>
 cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s) {
   const dim3 block(32, 8);
   const dim3 grid((nx + 31) / 32, (ny + 7) / 8, nz);
-  k_init<S><<<grid, block, 0, s>>>(a);
+  if (a.qf == kQ27) k_init<S, kQ27><<<grid, block, 0, s>>>(a);
+  else k_init<S, kQ><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1213,15 +1246,17 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
                                       const void* tmap, cudaStream_t s) {                  \
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
+    if (a.qf == kQ27)                                                                      \
+      return launch_on(collide27_kernel<S>(gmode), a.grid_collide, dim3(32, 8), a, s);     \
     dim3 block;                                                                            \
     const void* fn = collide_kernel_gm<S>(variant, gmode, &block);                         \
     return launch_on(fn, a.grid_collide, block, a, s);                                     \
   }                                                                                        \
   cudaError_t prepare_tma_##suffix() { return prepare_tma_kernel<S>(); }                   \
   size_t tma_smem_##suffix() { return TmaBox<typename S::FT>::kSmem; }                     \
-  cudaError_t occupancy_##suffix(int variant, int gmode, int* phi_blocks,                  \
+  cudaError_t occupancy_##suffix(int variant, int gmode, int qf, int* phi_blocks,          \
                                  int* collide_blocks) {                                    \
-    return occupancy_of<S>(variant, gmode, phi_blocks, collide_blocks);                    \
+    return occupancy_of<S>(variant, gmode, qf, phi_blocks, collide_blocks);                \
   }                                                                                        \
   cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
                                    cudaStream_t s) {                                       \

@@ -1,9 +1,11 @@
-// D3Q19 lattice constants shared by host and device code.
+// D3Q19 and D3Q27 lattice constants shared by host and device code.
 //
-// The population order is the reference's (src/var.cu:29-31): rest, the six faces, then
-// the twelve edges, with opposite pairs (1,2), (3,4), ..., (17,18). The weights are 1/3,
-// 1/18 and 1/36 (src/var.cu:40-45) and cs^2 = 1/3 (src/var.cu:22). Every index below is a
-// compile-time constant at its use, so the tables fold away in the kernels.
+// The population order is the reference's (src/var.cu:29-35): rest, the six faces, the
+// twelve edges, then (D3Q27 only) the eight corners, with opposite pairs (1,2), (3,4), ...,
+// (25,26). D3Q19 weights are 1/3, 1/18 and 1/36 (src/var.cu:40-45); D3Q27 weights are
+// 8/27, 2/27, 1/54 and 1/216 (src/var.cu:47-52); cs^2 = 1/3 for both (src/var.cu:22).
+// Every index below is a compile-time constant at its use, so the tables fold away in the
+// kernels. g and the phi stencils always use D3Q19; f uses D3Q19 or D3Q27.
 #pragma once
 
 #include <type_traits>
@@ -19,17 +21,25 @@ namespace mcb {
 
 constexpr int kQ = 19;
 
+constexpr int kQ27 = 27;
+
 MCB_HD constexpr int cx(int l) {
-  return (l == 1 || l == 7 || l == 9 || l == 13 || l == 15) ? 1
-       : (l == 2 || l == 8 || l == 10 || l == 14 || l == 16) ? -1 : 0;
+  return (l == 1 || l == 7 || l == 9 || l == 13 || l == 15 || l == 19 || l == 21 || l == 23 ||
+          l == 26) ? 1
+       : (l == 2 || l == 8 || l == 10 || l == 14 || l == 16 || l == 20 || l == 22 || l == 24 ||
+          l == 25) ? -1 : 0;
 }
 MCB_HD constexpr int cy(int l) {
-  return (l == 3 || l == 7 || l == 11 || l == 14 || l == 17) ? 1
-       : (l == 4 || l == 8 || l == 12 || l == 13 || l == 18) ? -1 : 0;
+  return (l == 3 || l == 7 || l == 11 || l == 14 || l == 17 || l == 19 || l == 21 || l == 24 ||
+          l == 25) ? 1
+       : (l == 4 || l == 8 || l == 12 || l == 13 || l == 18 || l == 20 || l == 22 || l == 23 ||
+          l == 26) ? -1 : 0;
 }
 MCB_HD constexpr int cz(int l) {
-  return (l == 5 || l == 9 || l == 11 || l == 16 || l == 18) ? 1
-       : (l == 6 || l == 10 || l == 12 || l == 15 || l == 17) ? -1 : 0;
+  return (l == 5 || l == 9 || l == 11 || l == 16 || l == 18 || l == 19 || l == 22 || l == 23 ||
+          l == 25) ? 1
+       : (l == 6 || l == 10 || l == 12 || l == 15 || l == 17 || l == 20 || l == 21 || l == 24 ||
+          l == 26) ? -1 : 0;
 }
 // Opposite direction: pairs (2k-1, 2k).
 MCB_HD constexpr int opp(int l) { return l == 0 ? 0 : ((l & 1) ? l + 1 : l - 1); }
@@ -40,6 +50,16 @@ MCB_HD constexpr float wf(int l) {
 }
 MCB_HD constexpr double wd(int l) {
   return l == 0 ? (1.0 / 3.0) : (l <= 6 ? (1.0 / 18.0) : (1.0 / 36.0));
+}
+// Weights of the f lattice (QF = 19 or 27).
+template <int QF>
+MCB_HD constexpr float wfq(int l) {
+  if constexpr (QF == 19) {
+    return wf(l);
+  } else {
+    return l == 0 ? (8.0f / 27.0f)
+         : (l <= 6 ? (2.0f / 27.0f) : (l <= 18 ? (1.0f / 54.0f) : (1.0f / 216.0f)));
+  }
 }
 
 // Exact integer split of a Q2.30 phi value over the 19 weights, for the weight part of the

@@ -51,7 +51,8 @@ class Config(C.Structure):
                 ("storage", C.c_int), ("tau", C.c_float), ("tau_g", C.c_float),
                 ("sigma", C.c_float), ("width", C.c_float), ("sharp_c", C.c_float),
                 ("gravity", C.c_float), ("device", C.c_int), ("variant", C.c_int),
-                ("zchunk", C.c_int), ("use_graph", C.c_int), ("g_mode", C.c_int)]
+                ("zchunk", C.c_int), ("use_graph", C.c_int), ("g_mode", C.c_int),
+                ("velocity_set", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

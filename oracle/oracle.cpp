@@ -24,6 +24,11 @@
 //     walls for the stencils.
 // Modes 1 and 2, BGK g relaxation with tau_g != 1 and the Boussinesq force have no
 // reference counterpart. They restate the same update with those additions.
+//
+// f on D3Q27 (qf = 27) uses the tables of src/var.cu:33-35,47-52. The reference's D3Q27
+// moments are unfinished (src/lbm.cu:174-218 keep D3Q19 index sums), so for it the moments
+// are taken from their definitions: rho = sum f, rho u = sum c f + F/2, and
+// Pi = sum c c (f - feq + F_l/2). g and the phi stencils stay on D3Q19.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -41,12 +46,20 @@ const int CIX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 
 const int CIY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1};
 const int CIZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1};
 int OPP(int l) { return l == 0 ? 0 : ((l & 1) ? l + 1 : l - 1); }
+// f lattice: D3Q19 followed by the eight D3Q27 corners (src/var.cu:33-35).
+const int FCX[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0,
+                     1, -1, 1, -1, 1, -1, -1, 1};
+const int FCY[27] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1,
+                     1, -1, 1, -1, -1, 1, 1, -1};
+const int FCZ[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1,
+                     1, -1, -1, 1, 1, -1, 1, -1};
 
 struct Params {
   int nx, ny, nz, bc;
   double tau, tau_g, sigma, sharp_c, gravity;
   int threads;
   int moving_wall;  // ref mode: also run movingWallBC's shell writes
+  int qf;           // velocity set of f: 19 or 27
 };
 
 template <class T>
@@ -54,6 +67,8 @@ struct Oracle {
   Params p;
   long long n;
   T W[19];
+  T FW[27];  // f weights (D3Q19 or D3Q27)
+  int QF;
   T CSSQ, OMEGA, OMEGA_G, SHARP_C, SIGMA;
   std::vector<T> f, g, g_out, phi, nx_, ny_, nz_, ind, curv, ffx, ffy, ffz;
   std::vector<T> ux, uy, uz, rho, pxx, pyy, pzz, pxy, pxz, pyz;
@@ -65,13 +80,22 @@ struct Oracle {
     W[0] = T(1) / T(3);
     for (int l = 1; l <= 6; ++l) W[l] = T(1) / T(18);
     for (int l = 7; l < 19; ++l) W[l] = T(1) / T(36);
+    QF = p.qf == 27 ? 27 : 19;
+    if (QF == 19) {
+      for (int l = 0; l < 19; ++l) FW[l] = W[l];
+    } else {
+      FW[0] = T(8) / T(27);
+      for (int l = 1; l <= 6; ++l) FW[l] = T(2) / T(27);
+      for (int l = 7; l < 19; ++l) FW[l] = T(1) / T(54);
+      for (int l = 19; l < 27; ++l) FW[l] = T(1) / T(216);
+    }
     CSSQ = T(1) / T(3);
     OMEGA = T(1) / T(p.tau);
     OMEGA_G = T(1) / T(p.tau_g);
     SHARP_C = T(p.sharp_c);
     SIGMA = T(p.sigma);
     const size_t N = static_cast<size_t>(n);
-    f.assign(19 * N, 0);
+    f.assign(static_cast<size_t>(QF) * N, 0);
     g.assign(19 * N, 0);
     g_out.assign(19 * N, 0);
     for (auto* v : {&phi, &nx_, &ny_, &nz_, &ind, &curv, &ffx, &ffy, &ffz, &ux, &uy, &uz, &rho,
@@ -152,9 +176,12 @@ struct Oracle {
       const long long o = I3(i, j, k);
       const T a = ux[o], b = uy[o], c = uz[o];
       const T uu = T(1.5) * (a * a + b * b + c * c);
+      for (int l = 0; l < QF; ++l) {
+        const T cu = T(3) * (a * FCX[l] + b * FCY[l] + c * FCZ[l]);
+        f[I4(i, j, k, l)] = FW[l] * rho[o] * (T(1) + cu + T(0.5) * cu * cu - uu);
+      }
       for (int l = 0; l < 19; ++l) {
         const T cu = T(3) * (a * CIX[l] + b * CIY[l] + c * CIZ[l]);
-        f[I4(i, j, k, l)] = W[l] * rho[o] * (T(1) + cu + T(0.5) * cu * cu - uu);
         g[I4(i, j, k, l)] = W[l] * phi[o] * (T(1) + cu);
       }
     });
@@ -219,8 +246,60 @@ struct Oracle {
     });
   }
 
+  // Moments of D3Q27 f from their definitions (see the header).
+  void moments_q27() {
+    for_cells([&](int i, int j, int k) {
+      if (!acts(i, j, k)) return;
+      const long long o = I3(i, j, k);
+      T fv[27];
+      for (int l = 0; l < 27; ++l) fv[l] = f[I4(i, j, k, l)];
+      T r = 0, jx = 0, jy = 0, jz = 0;
+      for (int l = 0; l < 27; ++l) {
+        r += fv[l];
+        jx += FCX[l] * fv[l];
+        jy += FCY[l] * fv[l];
+        jz += FCZ[l] * fv[l];
+      }
+      const T inv = T(1) / r;
+      const T fx = ffx[o], fy = ffy[o], fz = ffz[o];
+      const T a = (jx + T(0.5) * fx) * inv, b = (jy + T(0.5) * fy) * inv;
+      const T c = (jz + T(0.5) * fz) * inv;
+      const T ic = T(1) / CSSQ;
+      const T uu = T(0.5) * (a * a + b * b + c * c) * ic;
+      const T irc = T(1) / (r * CSSQ);
+      T sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+      for (int l = 0; l < 27; ++l) {
+        const T udc = (a * FCX[l] + b * FCY[l] + c * FCZ[l]) * ic;
+        const T common = FW[l] * (r + r * (udc + T(0.5) * udc * udc - uu));
+        const T hef = T(0.5) * common *
+                      ((FCX[l] - a) * fx + (FCY[l] - b) * fy + (FCZ[l] - c) * fz) * irc;
+        const T fneq = fv[l] - (common - hef);
+        sxx += FCX[l] * FCX[l] * fneq;
+        syy += FCY[l] * FCY[l] * fneq;
+        szz += FCZ[l] * FCZ[l] * fneq;
+        sxy += FCX[l] * FCY[l] * fneq;
+        sxz += FCX[l] * FCZ[l] * fneq;
+        syz += FCY[l] * FCZ[l] * fneq;
+      }
+      pxx[o] = sxx;
+      pyy[o] = syy;
+      pzz[o] = szz;
+      pxy[o] = sxy;
+      pxz[o] = sxz;
+      pyz[o] = syz;
+      ux[o] = a;
+      uy[o] = b;
+      uz[o] = c;
+      rho[o] = r;
+    });
+  }
+
   // momentiCalc, src/lbm.cu:133-225.
   void momenti_calc() {
+    if (QF == 27) {
+      moments_q27();
+      return;
+    }
     for_cells([&](int i, int j, int k) {
       if (!acts(i, j, k)) return;
       const long long o = I3(i, j, k);
@@ -267,9 +346,9 @@ struct Oracle {
   // Target of a push along direction l from (i,j,k): false if the link leaves through a
   // z wall (the population bounces back into (i,j,k) as opp(l)).
   bool push_target(int i, int j, int k, int l, int& ti, int& tj, int& tk) const {
-    ti = i + CIX[l];
-    tj = j + CIY[l];
-    tk = k + CIZ[l];
+    ti = i + FCX[l];
+    tj = j + FCY[l];
+    tk = k + FCZ[l];
     if (ref()) return true;  // interior cells always land inside
     ti = wrap(ti, p.nx);
     tj = wrap(tj, p.ny);
@@ -288,15 +367,15 @@ struct Oracle {
       const T uu = T(0.5) * (a * a + b * b + c * c) / CSSQ;
       const T irc = T(1) / (r * CSSQ);
       const T ic = T(1) / CSSQ;
-      for (int l = 0; l < 19; ++l) {
-        const T udc = (a * CIX[l] + b * CIY[l] + c * CIZ[l]) * ic;
-        const T feq = W[l] * (r + r * (udc + T(0.5) * udc * udc - uu));
-        const T hef = T(0.5) * feq *
-                      ((CIX[l] - a) * fx + (CIY[l] - b) * fy + (CIZ[l] - c) * fz) * irc;
-        const T fneq = (W[l] / (T(2) * CSSQ * CSSQ)) *
-                       ((CIX[l] * CIX[l] - CSSQ) * pxx[o] + (CIY[l] * CIY[l] - CSSQ) * pyy[o] +
-                        (CIZ[l] * CIZ[l] - CSSQ) * pzz[o] + T(2) * CIX[l] * CIY[l] * pxy[o] +
-                        T(2) * CIX[l] * CIZ[l] * pxz[o] + T(2) * CIY[l] * CIZ[l] * pyz[o]);
+      for (int l = 0; l < QF; ++l) {
+        const int X = FCX[l], Y = FCY[l], Z = FCZ[l];
+        const T udc = (a * X + b * Y + c * Z) * ic;
+        const T feq = FW[l] * (r + r * (udc + T(0.5) * udc * udc - uu));
+        const T hef = T(0.5) * feq * ((X - a) * fx + (Y - b) * fy + (Z - c) * fz) * irc;
+        const T fneq = (FW[l] / (T(2) * CSSQ * CSSQ)) *
+                       ((X * X - CSSQ) * pxx[o] + (Y * Y - CSSQ) * pyy[o] +
+                        (Z * Z - CSSQ) * pzz[o] + T(2) * X * Y * pxy[o] +
+                        T(2) * X * Z * pxz[o] + T(2) * Y * Z * pyz[o]);
         const T post = feq + (T(1) - OMEGA) * fneq + hef;
         int ti, tj, tk;
         if (push_target(i, j, k, l, ti, tj, tk)) f[I4(ti, tj, tk, l)] = post;
@@ -335,11 +414,11 @@ struct Oracle {
     const T uw = T(0.03);
     for (int k = 0; k < kmax; ++k)
       for (int i = 0; i < p.nx; ++i)
-        for (int l = 0; l < 19; ++l) {
+        for (int l = 0; l < QF; ++l) {
           const T rb = rho[I3(i, 0, k)];
-          f[I4(i, 0, k, l)] = rb * W[l] * (T(1) + (CIX[l] * (-uw)) / CSSQ);
+          f[I4(i, 0, k, l)] = rb * FW[l] * (T(1) + (FCX[l] * (-uw)) / CSSQ);
           const T rt = rho[I3(i, p.ny - 1, k)];
-          f[I4(i, p.ny - 1, k, l)] = rt * W[l] * (T(1) + (CIX[l] * uw) / CSSQ);
+          f[I4(i, p.ny - 1, k, l)] = rt * FW[l] * (T(1) + (FCX[l] * uw) / CSSQ);
         }
   }
 
@@ -368,10 +447,10 @@ struct Oracle {
         for (int i = 0; i < p.nx; ++i) {
           if (!shell(i, j, k)) continue;
           const long long o = I3(i, j, k);
-          for (int l = 0; l < 19; ++l) {
-            const int a = i + CIX[l], b = j + CIY[l], c = k + CIZ[l];
+          for (int l = 0; l < QF; ++l) {
+            const int a = i + FCX[l], b = j + FCY[l], c = k + FCZ[l];
             if (a >= 0 && a < p.nx && b >= 0 && b < p.ny && c >= 0 && c < p.nz)
-              f[I4(a, b, c, l)] = rho[o] * W[l];
+              f[I4(a, b, c, l)] = rho[o] * FW[l];
           }
           for (int l = 0; l < 19; ++l) {
             const int a = i + CIX[l], b = j + CIY[l], c = k + CIZ[l];
@@ -439,13 +518,15 @@ typedef struct orc_params {
   double tau, tau_g, sigma, sharp_c, gravity;
   int threads;
   int moving_wall;
+  int qf;  // velocity set of f: 19 (or 0) or 27
 } orc_params;
 
 void* orc_create(const orc_params* q, int precision) {
   if (!q || q->nx < 3 || q->ny < 3 || q->nz < 3 || q->bc < 0 || q->bc > 2) return nullptr;
   if (precision != 32 && precision != 64) return nullptr;
+  if (q->qf != 0 && q->qf != 19 && q->qf != 27) return nullptr;
   Params p{q->nx, q->ny, q->nz, q->bc, q->tau, q->tau_g, q->sigma, q->sharp_c, q->gravity,
-           q->threads > 0 ? q->threads : 1, q->moving_wall};
+           q->threads > 0 ? q->threads : 1, q->moving_wall, q->qf == 27 ? 27 : 19};
   Any* a = new Any{precision, nullptr};
   if (precision == 64) a->impl = new Oracle<double>(p);
   else a->impl = new Oracle<float>(p);

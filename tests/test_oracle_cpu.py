@@ -162,3 +162,77 @@ def test_node_centred_bubble_amplifies_rounding(built):
     for o in runs:
         o.step(6)
     assert np.max(np.abs(runs[0].get("phi") - runs[1].get("phi"))) > 1e-4
+
+
+# D3Q27 f (src/var.cu:33-35, 47-52): the D3Q19 set followed by the eight corners.
+CX27 = np.concatenate([CX, [1, -1, 1, -1, 1, -1, -1, 1]])
+CY27 = np.concatenate([CY, [1, -1, 1, -1, -1, 1, 1, -1]])
+CZ27 = np.concatenate([CZ, [1, -1, -1, 1, 1, -1, 1, -1]])
+W27 = np.array([8 / 27] + [2 / 27] * 6 + [1 / 54] * 12 + [1 / 216] * 8)
+C27 = np.stack([CX27, CY27, CZ27], 1).astype(np.float64)
+
+
+def test_d3q27_tables_are_a_symmetric_isotropic_lattice():
+    """Opposite pairs (2k-1, 2k) and 4th-order isotropy: the closed-form moments of the
+    fused kernel hold for D3Q27 as for D3Q19."""
+    for l in range(1, 27, 2):
+        assert np.array_equal(C27[l], -C27[l + 1])
+    assert len({tuple(c) for c in C27}) == 27
+    cs2 = 1 / 3
+    assert np.isclose(W27.sum(), 1)
+    assert np.allclose(np.einsum("l,la,lb->ab", W27, C27, C27), cs2 * np.eye(3))
+    m4 = np.einsum("l,la,lb,lc,ld->abcd", W27, C27, C27, C27, C27)
+    d = np.eye(3)
+    want = cs2**2 * (np.einsum("ab,cd->abcd", d, d) + np.einsum("ac,bd->abcd", d, d)
+                     + np.einsum("ad,bc->abcd", d, d))
+    assert np.allclose(m4, want)
+    assert np.allclose(np.einsum("l,la,lb,lc->abc", W27, C27, C27, C27), 0)
+
+
+def _shear_wave(velocity_set, tau=0.8, n=32, amp=1e-4, steps=300):
+    """u_x = amp sin(2 pi z / n) in a single phase; returns the fitted decay rate and the
+    analytic nu k^2, nu = cs^2 (tau - 1/2)."""
+    nx, ny, nz = 4, 4, n
+    z = np.arange(nz)
+    ux = np.broadcast_to((amp * np.sin(2 * np.pi * z / nz))[:, None, None],
+                         (nz, ny, nx)).astype(np.float32)
+    zero = np.zeros((nz, ny, nx), np.float32)
+    o = Oracle(nx, ny, nz, mcb.BC_PERIODIC, tau, 1.0, 0.0, 0.0, velocity_set=velocity_set)
+    o.set_fields(zero, ux, zero, zero)
+    o.step(steps)
+    got = o.get("ux")[:, 0, 0]
+    o.close()
+    # the initial profile is u at update 0's start; steps updates decay it steps times
+    a = np.dot(got, np.sin(2 * np.pi * z / nz)) / np.dot(np.sin(2 * np.pi * z / nz),
+                                                       np.sin(2 * np.pi * z / nz))
+    rate = -np.log(a / amp) / steps
+    nu = (tau - 0.5) / 3
+    return rate, nu * (2 * np.pi / nz) ** 2
+
+
+@pytest.mark.parametrize("velocity_set", [19, 27])
+def test_shear_wave_decays_at_the_lattice_viscosity(built, velocity_set):
+    rate, want = _shear_wave(velocity_set)
+    assert rate == pytest.approx(want, rel=2e-3)
+
+
+def test_d3q27_rest_state_stays_fixed_and_conserves_mass(built):
+    n = 12
+    phi = np.full((n, n, n), 0.3, np.float32)
+    o = Oracle(n, n, n, mcb.BC_PERIODIC, 0.7, 1.0, 0.05, 0.5, velocity_set=27)
+    o.set_fields(phi)
+    o.step(20)
+    assert np.max(np.abs(o.get("ux"))) < 1e-15
+    assert np.max(np.abs(o.get("rho") - 1)) < 1e-14
+    assert np.max(np.abs(o.get("phi") - np.float32(0.3))) < 1e-14
+    o.close()
+    cfg, phi, *_ = mcb.workload(1, scale=0.25)  # 16^3 static bubble, periodic
+    cfg.velocity_set = 27
+    o = Oracle.from_config(cfg)
+    o.set_fields(phi)
+    o.step(1)
+    r0, m0 = o.get("rho").sum(), o.diagnostics()["mass"]
+    o.step(40)
+    assert o.get("rho").sum() == pytest.approx(r0, rel=1e-12)
+    assert o.diagnostics()["mass"] == pytest.approx(m0, rel=1e-12)
+    o.close()
