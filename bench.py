@@ -289,6 +289,27 @@ def batch_run(device, steps, ncases=64):
             "speedup": ms_seq / ms_batch}
 
 
+def d3q27_run(device, steps, storage="f32"):
+    """The same workload with f on D3Q27 (27 populations): device MLUPS."""
+    import mcb
+
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=SCALE)
+    cfg.storage = mcb.STORAGES[storage]
+    cfg.velocity_set = 27
+    cfg.device = device
+    cells = cfg.nx * cfg.ny * cfg.nz
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi, ux, uy, uz)
+        s.step(20)
+        total, t_phi, t_col = s.step_profiled(steps)
+    pb = 4 if storage == "f32" else 2
+    col_bytes = 2 * 27 * pb + 4 + 16 + (4 if storage != "f32" else 0)
+    return {"storage": storage, "steps": steps, "mlups": cells * steps / (total * 1e-3) / 1e6,
+            "kernel_ms": {"k_phi": t_phi / steps, "k_collide": t_col / steps},
+            "collide_bytes_per_lu": col_bytes,
+            "collide_gbs_algorithmic": col_bytes * cells / (t_col * 1e-3 / steps) / 1e9}
+
+
 def swarm_run(device, steps):
     """The large swarm: 512^3, FP16 storage, walls in z, gravity 5e-6, 512 bubbles."""
     import mcb
@@ -465,6 +486,7 @@ def main():
         if not args.no_extras:
             result["batch"] = batch_run(local, min(args.steps, 200))
             result["swarm"] = swarm_run(local, min(args.steps, 50))
+            result["d3q27"] = [d3q27_run(local, min(args.steps, 200), st) for st in ("f32", "f16")]
         result["reference_cuda"] = reference_cuda_run(local, min(args.steps, 200))
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         print(json.dumps(result))

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MCB_ABI_VERSION 3
+#define MCB_ABI_VERSION 4
 
 /* status codes */
 #define MCB_OK            0
@@ -97,6 +97,14 @@ typedef struct mcb_config {
                            reference's D3Q27 moments are unfinished, src/lbm.cu:174-218).
                            g and the phi stencils are D3Q19 either way. D3Q27 runs the
                            32x8 tile. */
+    float rho_in;       /* density of the phi = 1 phase (the bubble) */
+    float rho_out;      /* density of the phi = 0 phase. rho_in == rho_out (default 1, 1)
+                           runs the reference's density-matched update; otherwise f carries
+                           the normalised pressure p / (rho cs^2) of the velocity-based
+                           density-ratio formulation (Zu and He 2013; Fakhari et al. 2017),
+                           with rho = rho_out + (rho_in - rho_out) phi, one kinematic
+                           viscosity, and MCB_FIELD_RHO reporting p / cs^2. Periodic and
+                           wall modes only; runs the 32x8 tile. */
 } mcb_config;
 
 #define MCB_G_AUTO         0

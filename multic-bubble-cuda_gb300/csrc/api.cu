@@ -90,6 +90,13 @@ int validate(const mcb_config& c, int index) {
   if (c.velocity_set != 19 && c.velocity_set != 27)
     return fail(MCB_ERR_INVALID, "case %d: velocity_set must be 19 or 27 (got %d)", index,
                 c.velocity_set);
+  if (!(c.rho_in > 0.f) || !(c.rho_out > 0.f) || !std::isfinite(c.rho_in) ||
+      !std::isfinite(c.rho_out))
+    return fail(MCB_ERR_INVALID, "case %d: rho_in and rho_out must be > 0", index);
+  if (c.rho_in != c.rho_out && c.bc == MCB_BC_REF)
+    return fail(MCB_ERR_INVALID,
+                "case %d: the reference boundary mode is density-matched (rho_in == rho_out)",
+                index);
   if (c.zchunk < -kMaxWaves)
     return fail(MCB_ERR_INVALID, "case %d: zchunk must be >= -%d", index, kMaxWaves);
   if (c.g_mode != MCB_G_AUTO && c.g_mode != MCB_G_POPULATIONS)
@@ -112,6 +119,7 @@ struct Solver {
   bool bgk = false;
   int gmode = mcb::kGPop;
   int qf = 19;             // velocity set of f
+  int ratio = 0;           // density-ratio model
   bool padded = false;     // f in the padded layout of the TMA collide
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
@@ -232,7 +240,7 @@ struct Solver {
       const int waves = -zchunk;
       int nsm = 0, occ_phi = 0, occ_col = 0;
       MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, &occ_phi, &occ_col));
+      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, &occ_phi, &occ_col));
       if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
         return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
       grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
@@ -256,10 +264,13 @@ struct Solver {
     storage = cs[0].storage;
     device = cs[0].device;
     qf = cs[0].velocity_set;
+    ratio = cs[0].rho_in != cs[0].rho_out;
     for (int i = 1; i < n; ++i)
-      if (cs[i].storage != storage || cs[i].device != device || cs[i].velocity_set != qf)
+      if (cs[i].storage != storage || cs[i].device != device || cs[i].velocity_set != qf ||
+          (cs[i].rho_in != cs[i].rho_out) != (ratio != 0))
         return fail(MCB_ERR_INVALID,
-                    "all cases of a batch must share storage, device and velocity set");
+                    "all cases of a batch must share storage, device, velocity set and "
+                    "density model");
     // Default tile from measured sweeps on GB300: 32x8 (either storage).
     variant = cs[0].variant >= 0 ? cs[0].variant : 0;
     zchunk_req = cs[0].zchunk;
@@ -285,6 +296,8 @@ struct Solver {
       d.sharp_c = sharp_of(c);
       d.gravity = c.gravity;
       d.phi_mean = 0.f;
+      d.rho_out = ratio ? c.rho_out : 1.0f;
+      d.drho = ratio ? c.rho_in - c.rho_out : 0.0f;
       off += d.ncell;
       max_cells = std::max(max_cells, d.ncell);
       if (c.tau_g != 1.0f) bgk = true;
@@ -299,10 +312,11 @@ struct Solver {
     // runs the plain 32x8 tile.
     // Ghost columns: 32 bytes on each side keep every row's cells on 32-byte sectors.
     const int gxe = 32 / static_cast<int>(pop_bytes(storage));
-    padded = n == 1 && qf == 19 && gmode == mcb::kGEquil && cs[0].nx % (gxe / 2) == 0 &&
+    padded = n == 1 && qf == 19 && !ratio && gmode == mcb::kGEquil &&
+             cs[0].nx % (gxe / 2) == 0 &&
              cs[0].variant == mcb::kTmaVariant && encode_fn() != nullptr;
     if (padded) variant = mcb::kTmaVariant;
-    else if (variant == mcb::kTmaVariant || qf == 27) variant = 0;  // D3Q27: the 32x8 tile
+    else if (variant == mcb::kTmaVariant || qf == 27 || ratio) variant = 0;  // the 32x8 tile
     for (auto& d : cases) {
       if (padded) {
         d.fgx = gxe;
@@ -473,6 +487,7 @@ struct Solver {
     a.grid_collide = grid_collide;
     a.err = err;
     a.qf = qf;
+    a.ratio = ratio;
     a.f_in = f[parity];
     a.f_out = f[parity ^ 1];
     a.g_in = g[parity];
@@ -610,7 +625,7 @@ struct Solver {
   // ---- checkpoint: header + raw device buffers ----
   struct CkptHeader {
     char magic[8];
-    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad, qf;
+    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad, qf, ratio, pad2;
     long long update;
     float tau, tau_g, sigma, sharp_c, gravity, phi_mean;
   };
@@ -653,6 +668,7 @@ struct Solver {
     hd.latest_p = latest_p;
     hd.pad = padded ? cases[0].fgx : 0;  // f layout
     hd.qf = qf;
+    hd.ratio = ratio;
     hd.update = update;
     hd.tau = cfg[0].tau;
     hd.tau_g = cfg[0].tau_g;
@@ -694,11 +710,11 @@ struct Solver {
     mcb::CaseDesc& d = cases[0];
     if (hd.nx != d.nx || hd.ny != d.ny || hd.nz != d.nz || hd.bc != d.bc ||
         hd.storage != storage || hd.gmode != gmode || hd.pad != (padded ? d.fgx : 0) ||
-        hd.qf != qf) {
+        hd.qf != qf || hd.ratio != ratio) {
       std::fclose(fp);
       return fail(MCB_ERR_INVALID,
                   "checkpoint %s was written for another size, boundary mode, storage, g mode, "
-                  "f layout or velocity set",
+                  "f layout, velocity set or density model",
                   path);
     }
     MCB_CU(cudaStreamSynchronize(stream));
@@ -861,6 +877,8 @@ int mcb_config_default(mcb_config* c) {
   c->use_graph = 1;
   c->g_mode = MCB_G_AUTO;
   c->velocity_set = 19;
+  c->rho_in = 1.0f;
+  c->rho_out = 1.0f;
   return MCB_OK;
 }
 
@@ -1117,7 +1135,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     // The f layout is fixed at creation: the TMA variant alone on the padded layout, the
     // plain tiles otherwise.
     if ((v == mcb::kTmaVariant) != s.padded) continue;
-    if (s.qf == 27 && v != 0) continue;  // D3Q27 runs the 32x8 tile
+    if ((s.qf == 27 || s.ratio) && v != 0) continue;  // these run the 32x8 tile
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;
       s.variant = v;

@@ -24,11 +24,11 @@ cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, const
                                cudaStream_t s);
 cudaError_t prepare_tma_bf16();
 size_t tma_smem_bf16();
-cudaError_t occupancy_f32(int variant, int gmode, int qf, int* phi_blocks,
+cudaError_t occupancy_f32(int variant, int gmode, int qf, int ratio, int* phi_blocks,
                           int* collide_blocks);
-cudaError_t occupancy_f16(int variant, int gmode, int qf, int* phi_blocks,
+cudaError_t occupancy_f16(int variant, int gmode, int qf, int ratio, int* phi_blocks,
                           int* collide_blocks);
-cudaError_t occupancy_bf16(int variant, int gmode, int qf, int* phi_blocks,
+cudaError_t occupancy_bf16(int variant, int gmode, int qf, int ratio, int* phi_blocks,
                           int* collide_blocks);
 cudaError_t launch_init_f32(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_f16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
@@ -103,7 +103,11 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag(const DiagArgs a) {
     d.mass_q30 += P;
     const double u2 = static_cast<double>(ux) * ux + static_cast<double>(uy) * uy +
                       static_cast<double>(uz) * uz;
-    d.ke += 0.5 * static_cast<double>(rho) * u2;
+    // with a density ratio the rho field holds p / cs^2; the energy takes the density
+    const double rk = cd->drho != 0.f ? static_cast<double>(cd->rho_out) +
+                                            static_cast<double>(cd->drho) * phi
+                                      : static_cast<double>(rho);
+    d.ke += 0.5 * rk * u2;
     d.umax = fmax(d.umax, sqrt(u2));
     if (phi > 0.99f) { d.rho_in += rho; d.n_in += 1.0; }
     if (phi < 0.01f) { d.rho_out += rho; d.n_out += 1.0; }
@@ -232,12 +236,12 @@ size_t tma_smem_bytes(int storage) {
   }
 }
 
-cudaError_t occupancy(int storage, int variant, int gmode, int qf, int* phi_blocks,
+cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int* phi_blocks,
                       int* collide_blocks) {
   switch (storage) {
-    case kStF32: return occupancy_f32(variant, gmode, qf, phi_blocks, collide_blocks);
-    case kStF16: return occupancy_f16(variant, gmode, qf, phi_blocks, collide_blocks);
-    case kStBF16: return occupancy_bf16(variant, gmode, qf, phi_blocks, collide_blocks);
+    case kStF32: return occupancy_f32(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
+    case kStF16: return occupancy_f16(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
+    case kStBF16: return occupancy_bf16(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
     default: return cudaErrorInvalidValue;
   }
 }

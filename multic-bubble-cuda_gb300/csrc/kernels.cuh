@@ -568,10 +568,11 @@ __device__ __forceinline__ void f_ghosts(FT* f, long long fn, int x, int y, int 
 // ------------------------------------------------------- k_collide: the fused update --
 
 // QF: velocity set of f (19 or 27); g and the phi stencils are D3Q19 either way.
-template <class S, int GM, int BX, int BY, bool kTma = false, int QF = kQ>
+// kRatio: the density-ratio model (f carries p* = p / (rho cs^2); see DensityRatio below).
+template <class S, int GM, int BX, int BY, bool kTma = false, int QF = kQ, bool kRatio = false>
 __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t,
                                                 TmaPipe* pipe = nullptr) {
-  static_assert(QF == kQ || !kTma, "the TMA collide is D3Q19");
+  static_assert((QF == kQ && !kRatio) || !kTma, "the TMA collide is D3Q19, density-matched");
   constexpr bool BGK = GM == kGBgk;
   constexpr bool EQ = GM == kGEquil;
   using FT = typename S::FT;
@@ -595,6 +596,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   const float omega = __ldg(&cd->omega), omega_g = __ldg(&cd->omega_g);
   const float sigma = __ldg(&cd->sigma), sharp_c = __ldg(&cd->sharp_c);
   const float gravity = __ldg(&cd->gravity), phi_mean = __ldg(&cd->phi_mean);
+  const float rho_out = kRatio ? __ldg(&cd->rho_out) : 1.f, drho = kRatio ? __ldg(&cd->drho) : 0.f;
 
   const int* __restrict__ pcur = a.p_cur + t.cell_off;
 
@@ -822,8 +824,8 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     });
     const float phi = sphi[(z + 5) % 5][(ty + 2) * PX + tx + 2];
     const float mult = sigma * kap;
-    const float Fx = mult * nc.x * nc.w;
-    const float Fy = mult * nc.y * nc.w;
+    float Fx = mult * nc.x * nc.w;
+    float Fy = mult * nc.y * nc.w;
     float Fz = mult * nc.z * nc.w;
     if (gravity != 0.f) Fz += gravity * (phi - phi_mean);
 
@@ -840,7 +842,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       constexpr int L = decltype(LC)::value;
       f[L] = S::template f_raw<L>(fr[L]);
     });
-    constexpr float m0 = S::kFDev ? 1.0f : 0.0f, m2 = S::kFDev ? 1.0f / 3.0f : 0.0f;
+    // The density-ratio f is small (p* starts at 0) and is stored as it is.
+    constexpr bool kDevF = S::kFDev && !kRatio;
+    constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
     float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
     float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
     static_for<0, QF>([&](auto LC) {
@@ -854,19 +858,49 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
       if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
     });
-    const float inv_rho = 1.0f / rho;
-    const float ux = (jx + 0.5f * Fx) * inv_rho;
-    const float uy = (jy + 0.5f * Fy) * inv_rho;
-    const float uz = (jz + 0.5f * Fz) * inv_rho;
+    float ux, uy, uz, pxx, pyy, pzz, pxy, pxz, pyz, inv_rp = 0.f, rp = 1.f;
+    if constexpr (kRatio) {
+      // DensityRatio: velocity-based pressure formulation (Zu and He 2013; Fakhari et al.
+      // 2017) with rho = rho_out + drho phi and grad rho = drho grad phi, grad phi being
+      // n |grad phi| of the isotropic stencil.
+      //   p* = sum f, u* = sum c f, Pi* = sum c c f - p*/3 I - u* u*,
+      //   F += -p*/3 grad rho - (1 - omega/2) Pi* . grad rho,   u = u* + F / (2 rho).
+      rp = rho_out + drho * phi;
+      inv_rp = 1.0f / rp;
+      const float gx = drho * nc.x * nc.w, gy = drho * nc.y * nc.w, gz = drho * nc.z * nc.w;
+      const float p3 = rho * (1.0f / 3.0f);
+      const float qxx = sxx - p3 - jx * jx, qyy = syy - p3 - jy * jy, qzz = szz - p3 - jz * jz;
+      const float qxy = sxy - jx * jy, qxz = sxz - jx * jz, qyz = syz - jy * jz;
+      const float cm = 1.0f - 0.5f * omega;
+      Fx = Fx - p3 * gx - cm * (qxx * gx + qxy * gy + qxz * gz);
+      Fy = Fy - p3 * gy - cm * (qxy * gx + qyy * gy + qyz * gz);
+      Fz = Fz - p3 * gz - cm * (qxz * gx + qyz * gy + qzz * gz);
+      ux = jx + 0.5f * Fx * inv_rp;
+      uy = jy + 0.5f * Fy * inv_rp;
+      uz = jz + 0.5f * Fz * inv_rp;
+      pxx = sxx - p3 - ux * ux;
+      pyy = syy - p3 - uy * uy;
+      pzz = szz - p3 - uz * uz;
+      pxy = sxy - ux * uy;
+      pxz = sxz - ux * uz;
+      pyz = syz - uy * uz;
+    } else {
+      const float inv_rho = 1.0f / rho;
+      ux = (jx + 0.5f * Fx) * inv_rho;
+      uy = (jy + 0.5f * Fy) * inv_rho;
+      uz = (jz + 0.5f * Fz) * inv_rho;
+      const float uF = ux * Fx + uy * Fy + uz * Fz;
+      const float h = 1.5f * uF;
+      pxx = sxx - rho * (1.0f / 3.0f + ux * ux) + ux * Fx - h * ux * ux;
+      pyy = syy - rho * (1.0f / 3.0f + uy * uy) + uy * Fy - h * uy * uy;
+      pzz = szz - rho * (1.0f / 3.0f + uz * uz) + uz * Fz - h * uz * uz;
+      pxy = sxy - rho * ux * uy + 0.5f * (ux * Fy + uy * Fx) - h * ux * uy;
+      pxz = sxz - rho * ux * uz + 0.5f * (ux * Fz + uz * Fx) - h * ux * uz;
+      pyz = syz - rho * uy * uz + 0.5f * (uy * Fz + uz * Fy) - h * uy * uz;
+    }
     const float uF = ux * Fx + uy * Fy + uz * Fz;
     const float u2 = ux * ux + uy * uy + uz * uz;
     const float h = 1.5f * uF;
-    const float pxx = sxx - rho * (1.0f / 3.0f + ux * ux) + ux * Fx - h * ux * ux;
-    const float pyy = syy - rho * (1.0f / 3.0f + uy * uy) + uy * Fy - h * uy * uy;
-    const float pzz = szz - rho * (1.0f / 3.0f + uz * uz) + uz * Fz - h * uz * uz;
-    const float pxy = sxy - rho * ux * uy + 0.5f * (ux * Fy + uy * Fx) - h * ux * uy;
-    const float pxz = sxz - rho * ux * uz + 0.5f * (ux * Fz + uz * Fx) - h * ux * uz;
-    const float pyz = syz - rho * uy * uz + 0.5f * (uy * Fz + uz * Fy) - h * uy * uz;
     const float tr3 = (pxx + pyy + pzz) * (1.0f / 3.0f);
 
     // Regularized collision with He forcing (collisionFluid, src/lbm.cu:233-288):
@@ -876,9 +910,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     // c.u and c.F.
     const float om = (1.0f - omega) * 4.5f;
     // Deviation storage writes f*_l - W_l: the -1 folds into the shared term of each pair.
-    constexpr float fshift = S::kFDev ? -1.0f : 0.0f;
+    constexpr float fshift = kDevF ? -1.0f : 0.0f;
     const float R = rho - h;
-    const float base = 1.0f - 1.5f * u2;
+    // DensityRatio: f*_l = W_l [p* + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2 + 9/2 (1 - omega) Q_l:Pi
+    //                          + (1 - omega/2) 3 c.F / rho].
+    const float base = kRatio ? rho - 1.5f * u2 : 1.0f - 1.5f * u2;
+    const float cf = kRatio ? (1.0f - 0.5f * omega) * 3.0f * inv_rp : 0.f;
     // g collision (collisionPhase, src/lbm.cu:290-329):
     //   geq_l = W_l [phi (1 + 3 c.u) + sharp_c phi (1 - phi) c.n]
     // tau_g = 1 takes g* = geq as the reference does; otherwise BGK with omega_g.
@@ -887,7 +924,8 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
 
     float fo[QF];
     float go[kQ];
-    fo[0] = wfq<QF>(0) * (base * R - om * tr3 + fshift);
+    if constexpr (kRatio) fo[0] = wfq<QF>(0) * (base - om * tr3);
+    else fo[0] = wfq<QF>(0) * (base * R - om * tr3 + fshift);
     static_for<0, (QF - 1) / 2>([&](auto KC) {
       constexpr int L = 2 * decltype(KC)::value + 1;
       constexpr int O = L + 1;
@@ -902,8 +940,14 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       const float q = om * qp + fshift;
       const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
       const float rf = 1.5f * cF;
-      fo[L] = W * ((e0 + e1) * (R + rf) + q);
-      fo[O] = W * ((e0 - e1) * (R - rf) + q);
+      if constexpr (kRatio) {
+        const float fe = cf * cF;
+        fo[L] = W * (e0 + q + (e1 + fe));
+        fo[O] = W * (e0 + q - (e1 + fe));
+      } else {
+        fo[L] = W * ((e0 + e1) * (R + rf) + q);
+        fo[O] = W * ((e0 - e1) * (R - rf) + q);
+      }
       if constexpr (L < kQ) {
         constexpr float WG = wf(L);  // g is D3Q19
         const float dg = phi3 * cu + A * cn;
@@ -970,7 +1014,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     if (a.macros) {
       const long long T = a.cells_total, o = t.cell_off + idx;
       a.macros[o] = phi;
-      a.macros[T + o] = rho;
+      a.macros[T + o] = kRatio ? rho * rp : rho;  // density-ratio model: p / cs^2
       a.macros[2 * T + o] = ux;
       a.macros[3 * T + o] = uy;
       a.macros[4 * T + o] = uz;
@@ -1012,6 +1056,14 @@ template <class S, int GM>
 __global__ void __launch_bounds__(256, 2) k_collide27(const StepArgs a) {
   for_each_segment<32, 8, true>(
       a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27>(a, t); });
+}
+
+// Density-ratio model: 32x8 tiles; two blocks per SM for D3Q27 f, three for D3Q19.
+template <class S, int GM, int QF>
+__global__ void __launch_bounds__(256, QF == kQ27 ? 2 : kCollideWarpsPerSM / 8)
+    k_collide_ratio(const StepArgs a) {
+  for_each_segment<32, 8, true>(
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, QF, true>(a, t); });
 }
 
 // ------------------------------------------------------------------ k_init: fields --
@@ -1061,6 +1113,7 @@ __global__ void k_init(const InitArgs a) {
   const long long fidx =
       (static_cast<long long>(z) * cd->fpy + y + (cd->fgx ? 1 : 0)) * cd->fpx + x + cd->fgx;
   const bool fghost = cd->fgx != 0 && !ref;
+  const bool ratio = cd->drho != 0.f;
   GT* g0 = static_cast<GT*>(a.g0) + cd->g_off;
   static_for<0, QF>([&](auto LC) {
     constexpr int L = decltype(LC)::value;
@@ -1095,9 +1148,10 @@ __global__ void k_init(const InitArgs a) {
     const float cu = sx * ux + sy * uy + sz * uz;
     const float u2 = ux * ux + uy * uy + uz * uz;
     constexpr float W = wfq<QF>(L);
-    float feq = W * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
+    // density-ratio model: p* = 0 at the start, stored without the weight shift
+    float feq = W * ((ratio ? 0.0f : 1.0f) + 3.0f * cu + 4.5f * cu * cu - 1.5f * u2);
     if (shell) feq = W;
-    const float fst = S::kFDev ? feq - W : feq;
+    const float fst = (S::kFDev && !ratio) ? feq - W : feq;
     const FT v = S::template f_put<L>(fst);
     f0[L * fn + fidx] = v;
     f1[L * fn + fidx] = v;
@@ -1149,12 +1203,22 @@ const void* collide_kernel(int variant, dim3* block) {
   }
 }
 
+template <class S, int GM>
+const void* collide_32x8_kernel(int qf, bool ratio) {
+  if (ratio) {
+    return qf == kQ27 ? reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ27>)
+                      : reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ>);
+  }
+  return reinterpret_cast<const void*>(k_collide27<S, GM>);
+}
+
+// The 32x8 collide kernels outside the tile variants: D3Q27 f and the density-ratio model.
 template <class S>
-const void* collide27_kernel(int gmode) {
+const void* collide27_kernel(int gmode, int qf = kQ27, bool ratio = false) {
   switch (gmode) {
-    case kGPop: return reinterpret_cast<const void*>(k_collide27<S, kGPop>);
-    case kGBgk: return reinterpret_cast<const void*>(k_collide27<S, kGBgk>);
-    case kGEquil: return reinterpret_cast<const void*>(k_collide27<S, kGEquil>);
+    case kGPop: return collide_32x8_kernel<S, kGPop>(qf, ratio);
+    case kGBgk: return collide_32x8_kernel<S, kGBgk>(qf, ratio);
+    case kGEquil: return collide_32x8_kernel<S, kGEquil>(qf, ratio);
     default: return nullptr;
   }
 }
@@ -1194,15 +1258,16 @@ cudaError_t prepare_tma_kernel() {
 
 // Resident blocks per SM of the phi and collide kernels of a variant.
 template <class S>
-cudaError_t occupancy_of(int variant, int gmode, int qf, int* phi_blocks, int* collide_blocks) {
-  if (qf == kQ27) {
+cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int* phi_blocks,
+                         int* collide_blocks) {
+  if (qf == kQ27 || ratio) {
     dim3 bp;
     const void* fp = phi_kernel<S>(0, gmode == kGEquil, &bp);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(collide_blocks,
-                                                         collide27_kernel<S>(gmode), 256, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        collide_blocks, collide27_kernel<S>(gmode, qf, ratio != 0), 256, 0);
   }
   if (variant == kTmaVariant) {
     if (gmode != kGEquil) return cudaErrorInvalidValue;
@@ -1246,17 +1311,18 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
                                       const void* tmap, cudaStream_t s) {                  \
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
-    if (a.qf == kQ27)                                                                      \
-      return launch_on(collide27_kernel<S>(gmode), a.grid_collide, dim3(32, 8), a, s);     \
+    if (a.qf == kQ27 || a.ratio)                                                           \
+      return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0), a.grid_collide,     \
+                       dim3(32, 8), a, s);                                                 \
     dim3 block;                                                                            \
     const void* fn = collide_kernel_gm<S>(variant, gmode, &block);                         \
     return launch_on(fn, a.grid_collide, block, a, s);                                     \
   }                                                                                        \
   cudaError_t prepare_tma_##suffix() { return prepare_tma_kernel<S>(); }                   \
   size_t tma_smem_##suffix() { return TmaBox<typename S::FT>::kSmem; }                     \
-  cudaError_t occupancy_##suffix(int variant, int gmode, int qf, int* phi_blocks,          \
-                                 int* collide_blocks) {                                    \
-    return occupancy_of<S>(variant, gmode, qf, phi_blocks, collide_blocks);                \
+  cudaError_t occupancy_##suffix(int variant, int gmode, int qf, int ratio,                \
+                                 int* phi_blocks, int* collide_blocks) {                   \
+    return occupancy_of<S>(variant, gmode, qf, ratio, phi_blocks, collide_blocks);         \
   }                                                                                        \
   cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
                                    cudaStream_t s) {                                       \

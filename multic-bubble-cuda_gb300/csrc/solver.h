@@ -41,6 +41,8 @@ struct CaseDesc {
   float sharp_c;
   float gravity;
   float phi_mean;      // mean phi of the initial field (buoyancy reference)
+  float rho_out;       // density of phi = 0
+  float drho;          // rho_in - rho_out; nonzero selects the density-ratio model
 };
 
 // Buffers of one update. Populations are stored post-collision at the cell that
@@ -62,6 +64,7 @@ struct StepArgs {
   int grid_collide;    // blocks of the collide kernel
   int* err;            // set to a nonzero code when a bounded wait of a kernel gives up
   int qf;              // velocity set of f: 19 or 27 (every case of a launch)
+  int ratio;           // 1: the density-ratio model (every case of a launch)
   const void* f_in;   // 19 arrays per case
   void* f_out;
   const void* g_in;   // 18 moving g arrays per case (l = 1..18)
@@ -134,7 +137,7 @@ cudaError_t prepare_tma(int storage);
 // Dynamic shared memory of the TMA collide kernel for a storage.
 size_t tma_smem_bytes(int storage);
 // Resident blocks per SM of the phi and collide kernels of a tile variant.
-cudaError_t occupancy(int storage, int variant, int gmode, int qf, int* phi_blocks,
+cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int* phi_blocks,
                       int* collide_blocks);
 cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);

@@ -52,7 +52,7 @@ class Config(C.Structure):
                 ("sigma", C.c_float), ("width", C.c_float), ("sharp_c", C.c_float),
                 ("gravity", C.c_float), ("device", C.c_int), ("variant", C.c_int),
                 ("zchunk", C.c_int), ("use_graph", C.c_int), ("g_mode", C.c_int),
-                ("velocity_set", C.c_int)]
+                ("velocity_set", C.c_int), ("rho_in", C.c_float), ("rho_out", C.c_float)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

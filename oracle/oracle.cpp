@@ -29,6 +29,17 @@
 // moments are unfinished (src/lbm.cu:174-218 keep D3Q19 index sums), so for it the moments
 // are taken from their definitions: rho = sum f, rho u = sum c f + F/2, and
 // Pi = sum c c (f - feq + F_l/2). g and the phi stencils stay on D3Q19.
+//
+// Density ratio (rho_in != rho_out; periodic and wall modes): f carries the normalised
+// pressure p* = p / (rho cs^2) of the velocity-based formulation (Zu and He 2013; Fakhari,
+// Mitchell, Leonardi and Bolster 2017), with rho = rho_out + (rho_in - rho_out) phi:
+//   p* = sum f, u* = sum c f, Pi* = sum c c f - p* cs^2 I - u* u*,
+//   F = F_s + F_b - p* cs^2 grad rho - (1 - omega/2) Pi* . grad rho,
+//   u = u* + F / (2 rho),
+//   f*_l = W_l [p* + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2] + (1 - omega) W_l 9/2 Q_l : Pi
+//          + (1 - omega/2) 3 W_l c.F / rho,   Pi = sum c c f - p* cs^2 I - u u,
+// with grad rho = (rho_in - rho_out) grad phi from the isotropic stencil. The start is
+// p* = 0 at the given u. The rho field reports p / cs^2 = p* rho.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -60,6 +71,7 @@ struct Params {
   int threads;
   int moving_wall;  // ref mode: also run movingWallBC's shell writes
   int qf;           // velocity set of f: 19 or 27
+  double rho_in, rho_out;  // densities of phi = 1 and phi = 0 (equal: the reference model)
 };
 
 template <class T>
@@ -71,7 +83,7 @@ struct Oracle {
   int QF;
   T CSSQ, OMEGA, OMEGA_G, SHARP_C, SIGMA;
   std::vector<T> f, g, g_out, phi, nx_, ny_, nz_, ind, curv, ffx, ffy, ffz;
-  std::vector<T> ux, uy, uz, rho, pxx, pyy, pzz, pxy, pxz, pyz;
+  std::vector<T> ux, uy, uz, rho, pxx, pyy, pzz, pxy, pxz, pyz, pst;
   T phi_mean = 0;
   long long update = -1;
 
@@ -99,7 +111,7 @@ struct Oracle {
     g.assign(19 * N, 0);
     g_out.assign(19 * N, 0);
     for (auto* v : {&phi, &nx_, &ny_, &nz_, &ind, &curv, &ffx, &ffy, &ffz, &ux, &uy, &uz, &rho,
-                    &pxx, &pyy, &pzz, &pxy, &pxz, &pyz})
+                    &pxx, &pyy, &pzz, &pxy, &pxz, &pyz, &pst})
       v->assign(N, 0);
   }
 
@@ -108,6 +120,7 @@ struct Oracle {
   }
   long long I4(int i, int j, int k, int l) const { return I3(i, j, k) + n * l; }
   bool ref() const { return p.bc == 0; }
+  bool ratio() const { return p.rho_in != p.rho_out; }
   bool walls() const { return p.bc == 2; }
   bool shell(int i, int j, int k) const {
     return i == 0 || i == p.nx - 1 || j == 0 || j == p.ny - 1 || k == 0 || k == p.nz - 1;
@@ -167,7 +180,7 @@ struct Oracle {
           ux[o] = u ? T(u[o]) : T(0);
           uy[o] = v ? T(v[o]) : T(0);
           uz[o] = w ? T(w[o]) : T(0);
-          rho[o] = T(1);  // initTensor, src/init.cu:3-25
+          rho[o] = ratio() ? T(0) : T(1);  // initTensor, src/init.cu:3-25 (p* = 0)
         }
     phi_mean = T(sum / static_cast<double>(n));
     // initDist (src/init.cu:51-80), generalised to f at the equilibrium of u and
@@ -178,7 +191,8 @@ struct Oracle {
       const T uu = T(1.5) * (a * a + b * b + c * c);
       for (int l = 0; l < QF; ++l) {
         const T cu = T(3) * (a * FCX[l] + b * FCY[l] + c * FCZ[l]);
-        f[I4(i, j, k, l)] = FW[l] * rho[o] * (T(1) + cu + T(0.5) * cu * cu - uu);
+        // density ratio: p* = 0 at the start
+        f[I4(i, j, k, l)] = FW[l] * ((ratio() ? T(0) : rho[o]) + cu + T(0.5) * cu * cu - uu);
       }
       for (int l = 0; l < 19; ++l) {
         const T cu = T(3) * (a * CIX[l] + b * CIY[l] + c * CIZ[l]);
@@ -294,8 +308,60 @@ struct Oracle {
     });
   }
 
+  // Moments, total force and velocity of the density-ratio model (see the header).
+  void moments_ratio() {
+    const T drho = T(p.rho_in - p.rho_out), r_out = T(p.rho_out);
+    for_cells([&](int i, int j, int k) {
+      const long long o = I3(i, j, k);
+      T ps = 0, jx = 0, jy = 0, jz = 0, sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+      for (int l = 0; l < QF; ++l) {
+        const T v = f[I4(i, j, k, l)];
+        const T X = FCX[l], Y = FCY[l], Z = FCZ[l];
+        ps += v;
+        jx += X * v;
+        jy += Y * v;
+        jz += Z * v;
+        sxx += X * X * v;
+        syy += Y * Y * v;
+        szz += Z * Z * v;
+        sxy += X * Y * v;
+        sxz += X * Z * v;
+        syz += Y * Z * v;
+      }
+      const T rp = r_out + drho * phi[o];
+      const T gx = drho * nx_[o] * ind[o], gy = drho * ny_[o] * ind[o];
+      const T gz = drho * nz_[o] * ind[o];
+      const T p3 = ps * CSSQ;
+      const T qxx = sxx - p3 - jx * jx, qyy = syy - p3 - jy * jy, qzz = szz - p3 - jz * jz;
+      const T qxy = sxy - jx * jy, qxz = sxz - jx * jz, qyz = syz - jy * jz;
+      const T cm = T(1) - T(0.5) * OMEGA;
+      const T fx = ffx[o] - p3 * gx - cm * (qxx * gx + qxy * gy + qxz * gz);
+      const T fy = ffy[o] - p3 * gy - cm * (qxy * gx + qyy * gy + qyz * gz);
+      const T fz = ffz[o] - p3 * gz - cm * (qxz * gx + qyz * gy + qzz * gz);
+      const T a = jx + T(0.5) * fx / rp, b = jy + T(0.5) * fy / rp, c = jz + T(0.5) * fz / rp;
+      pxx[o] = sxx - p3 - a * a;
+      pyy[o] = syy - p3 - b * b;
+      pzz[o] = szz - p3 - c * c;
+      pxy[o] = sxy - a * b;
+      pxz[o] = sxz - a * c;
+      pyz[o] = syz - b * c;
+      ffx[o] = fx;
+      ffy[o] = fy;
+      ffz[o] = fz;
+      ux[o] = a;
+      uy[o] = b;
+      uz[o] = c;
+      pst[o] = ps;
+      rho[o] = ps * rp;  // p / cs^2
+    });
+  }
+
   // momentiCalc, src/lbm.cu:133-225.
   void momenti_calc() {
+    if (ratio()) {
+      moments_ratio();
+      return;
+    }
     if (QF == 27) {
       moments_q27();
       return;
@@ -357,8 +423,37 @@ struct Oracle {
     return true;
   }
 
+  // Collision of the density-ratio model (see the header), pushed like collisionFluid.
+  void collision_ratio() {
+    const T drho = T(p.rho_in - p.rho_out), r_out = T(p.rho_out);
+    for_cells([&](int i, int j, int k) {
+      const long long o = I3(i, j, k);
+      const T a = ux[o], b = uy[o], c = uz[o], ps = pst[o];
+      const T rp = r_out + drho * phi[o];
+      const T fx = ffx[o], fy = ffy[o], fz = ffz[o];
+      const T uu = T(1.5) * (a * a + b * b + c * c);
+      const T tr = (pxx[o] + pyy[o] + pzz[o]) * CSSQ;
+      for (int l = 0; l < QF; ++l) {
+        const int X = FCX[l], Y = FCY[l], Z = FCZ[l];
+        const T cu = T(3) * (a * X + b * Y + c * Z);
+        const T feq = FW[l] * (ps + cu + T(0.5) * cu * cu - uu);
+        const T qpi = X * X * pxx[o] + Y * Y * pyy[o] + Z * Z * pzz[o] +
+                      T(2) * (X * Y * pxy[o] + X * Z * pxz[o] + Y * Z * pyz[o]) - tr;
+        const T post = feq + (T(1) - OMEGA) * FW[l] * T(4.5) * qpi +
+                       (T(1) - T(0.5) * OMEGA) * T(3) * FW[l] * (X * fx + Y * fy + Z * fz) / rp;
+        int ti, tj, tk;
+        if (push_target(i, j, k, l, ti, tj, tk)) f[I4(ti, tj, tk, l)] = post;
+        else f[I4(i, j, k, OPP(l))] = post;
+      }
+    });
+  }
+
   // collisionFluid, src/lbm.cu:233-288 (in-place push; collision reads only the moments).
   void collision_fluid() {
+    if (ratio()) {
+      collision_ratio();
+      return;
+    }
     for_cells([&](int i, int j, int k) {
       if (!acts(i, j, k)) return;
       const long long o = I3(i, j, k);
@@ -519,14 +614,18 @@ typedef struct orc_params {
   int threads;
   int moving_wall;
   int qf;  // velocity set of f: 19 (or 0) or 27
+  double rho_in, rho_out;  // phase densities (0, 0 or equal: density-matched model)
 } orc_params;
 
 void* orc_create(const orc_params* q, int precision) {
   if (!q || q->nx < 3 || q->ny < 3 || q->nz < 3 || q->bc < 0 || q->bc > 2) return nullptr;
   if (precision != 32 && precision != 64) return nullptr;
   if (q->qf != 0 && q->qf != 19 && q->qf != 27) return nullptr;
+  const bool ratio = q->rho_in > 0 && q->rho_out > 0 && q->rho_in != q->rho_out;
+  if (ratio && q->bc == 0) return nullptr;  // the frozen shell is density-matched only
   Params p{q->nx, q->ny, q->nz, q->bc, q->tau, q->tau_g, q->sigma, q->sharp_c, q->gravity,
-           q->threads > 0 ? q->threads : 1, q->moving_wall, q->qf == 27 ? 27 : 19};
+           q->threads > 0 ? q->threads : 1, q->moving_wall, q->qf == 27 ? 27 : 19,
+           ratio ? q->rho_in : 1.0, ratio ? q->rho_out : 1.0};
   Any* a = new Any{precision, nullptr};
   if (precision == 64) a->impl = new Oracle<double>(p);
   else a->impl = new Oracle<float>(p);
@@ -587,10 +686,12 @@ int orc_diag(void* h, double* out) {
           if (o->ref() && o->shell(i, j, k)) continue;
           const long long c = o->I3(i, j, k);
           const double ph = o->phi[c], r = o->rho[c];
+          // kinetic energy with the density (the rho field is p / cs^2 with a ratio)
+          const double rk = o->ratio() ? o->p.rho_out + (o->p.rho_in - o->p.rho_out) * ph : r;
           const double u2 = double(o->ux[c]) * o->ux[c] + double(o->uy[c]) * o->uy[c] +
                             double(o->uz[c]) * o->uz[c];
           mass += ph;
-          ke += 0.5 * r * u2;
+          ke += 0.5 * rk * u2;
           umax = std::max(umax, std::sqrt(u2));
           if (ph > 0.99) { rin += r; nin += 1; }
           if (ph < 0.01) { rout += r; nout += 1; }

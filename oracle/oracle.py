@@ -24,7 +24,8 @@ class OrcParams(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("bc", C.c_int),
                 ("tau", C.c_double), ("tau_g", C.c_double), ("sigma", C.c_double),
                 ("sharp_c", C.c_double), ("gravity", C.c_double), ("threads", C.c_int),
-                ("moving_wall", C.c_int), ("qf", C.c_int)]
+                ("moving_wall", C.c_int), ("qf", C.c_int), ("rho_in", C.c_double),
+                ("rho_out", C.c_double)]
 
 
 _orc = None
@@ -63,10 +64,11 @@ class Oracle:
     """CPU restatement of the update. precision 64 (default) or 32."""
 
     def __init__(self, nx, ny, nz, bc, tau, tau_g, sigma, sharp_c, gravity=0.0,
-                 precision=64, threads=None, moving_wall=True, velocity_set=19):
+                 precision=64, threads=None, moving_wall=True, velocity_set=19, rho_in=1.0,
+                 rho_out=1.0):
         p = OrcParams(nx, ny, nz, bc, tau, tau_g, sigma, sharp_c, gravity,
                       threads or max(1, os.cpu_count() or 1), int(moving_wall),
-                      int(velocity_set))
+                      int(velocity_set), float(rho_in), float(rho_out))
         self._h = _orc_lib().orc_create(C.byref(p), precision)
         if not self._h:
             raise ValueError("orc_create rejected the parameters")
@@ -79,7 +81,8 @@ class Oracle:
         f = lambda v: float(np.float32(v))
         return cls(cfg.nx, cfg.ny, cfg.nz, cfg.bc, f(cfg.tau), f(cfg.tau_g), f(cfg.sigma),
                    f(np.float32(sharp_of(cfg))), f(cfg.gravity), precision, threads, moving_wall,
-                   getattr(cfg, "velocity_set", 19) or 19)
+                   getattr(cfg, "velocity_set", 19) or 19, f(getattr(cfg, "rho_in", 1.0) or 1.0),
+                   f(getattr(cfg, "rho_out", 1.0) or 1.0))
 
     def close(self):
         if self._h:

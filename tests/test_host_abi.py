@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(built):
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
     assert sorted(mcb.EXPORTS) == names
-    assert L.mcb_abi_version() == 3
+    assert L.mcb_abi_version() == 4
 
 
 def test_config_default_is_the_reference_case(built):
@@ -41,7 +41,8 @@ def test_config_default_is_the_reference_case(built):
 @pytest.mark.parametrize("field,value,needle", [
     ("nx", 2, "below 4"), ("tau", 0.4, "tau must"), ("tau_g", 0.5, "tau_g must"),
     ("bc", 7, "boundary"), ("storage", 9, "storage"), ("width", 0.0, "width"),
-    ("variant", 99, "variant"), ("zchunk", -17, "zchunk"), ("velocity_set", 15, "velocity_set")])
+    ("variant", 99, "variant"), ("zchunk", -17, "zchunk"), ("velocity_set", 15, "velocity_set"),
+    ("rho_in", 0.0, "rho_in")])
 def test_invalid_configs_are_rejected_before_touching_the_gpu(built, field, value, needle):
     c = mcb.default_config(bc=mcb.BC_PERIODIC, tau_g=1.0)
     setattr(c, field, value)

@@ -236,3 +236,30 @@ def test_d3q27_rest_state_stays_fixed_and_conserves_mass(built):
     assert o.get("rho").sum() == pytest.approx(r0, rel=1e-12)
     assert o.diagnostics()["mass"] == pytest.approx(m0, rel=1e-12)
     o.close()
+
+
+def test_density_ratio_oracle_static_bubble_obeys_laplace(built):
+    """The oracle's density-ratio model (ratio 10) on a 32^3 periodic static bubble:
+    dp = 2 sigma / R within 2 % and conserved phi mass."""
+    import math
+
+    n, r, sigma = 32, 8.0, 0.01
+    c = (n - 1) / 2
+    phi = mcb.fill_phi_bubbles(n, n, n, mcb.BC_PERIODIC, 4.0, [(c, c, c, r)])
+    o = Oracle(n, n, n, mcb.BC_PERIODIC, 0.8, 1.0, sigma, 0.5, rho_in=10.0, rho_out=1.0)
+    o.set_fields(phi)
+    o.step(1)
+    m0 = o.diagnostics()["mass"]
+    o.step(600)
+    d = o.diagnostics()
+    o.close()
+    rh = (3 * d["vol_half"] / (4 * math.pi)) ** (1 / 3)
+    assert abs(d["dp"] * rh / (2 * sigma) - 1) < 0.02
+    assert d["mass"] == pytest.approx(m0, rel=1e-12)
+    assert d["umax"] < 2e-5
+
+
+def test_density_ratio_is_refused_in_reference_mode(built):
+    c = mcb.default_config(rho_in=10.0, rho_out=1.0)
+    with pytest.raises(mcb.McbError, match="density-matched"):
+        mcb.Solver(c)
