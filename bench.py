@@ -165,6 +165,7 @@ class Clocks:
 
 SCALE = 1.0
 G_POPULATIONS = False
+VARIANT, ZCHUNK = -1, 0
 
 
 def make_solver(storage: str, device: int):
@@ -175,6 +176,7 @@ def make_solver(storage: str, device: int):
     cfg.device = device
     if G_POPULATIONS:
         cfg.g_mode = mcb.G_POPULATIONS
+    cfg.variant, cfg.zchunk = VARIANT, ZCHUNK
     s = mcb.Solver(cfg)
     return s, cfg, (phi, ux, uy, uz)
 
@@ -414,12 +416,17 @@ def main():
                     help="skip the batched-cases and 512^3 swarm legs")
     ap.add_argument("--g-populations", action="store_true",
                     help="store the 19 g populations instead of the (phi, J) records")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="tile variant of the device leg (-1 default; 4 the TMA-staged collide)")
+    ap.add_argument("--zchunk", type=int, default=0,
+                    help="work split of the device leg (0 default, >0 fixed chunks, -w waves)")
     ap.add_argument("--only-device", action="store_true",
                     help="time the device loop only (no fp16, e2e, reference or CPU legs)")
     args = ap.parse_args()
-    global SCALE, G_POPULATIONS
+    global SCALE, G_POPULATIONS, VARIANT, ZCHUNK
     SCALE = args.scale
     G_POPULATIONS = args.g_populations
+    VARIANT, ZCHUNK = args.variant, args.zchunk
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, ws, rank)
