@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -120,6 +121,7 @@ struct Solver {
   int gmode = mcb::kGPop;
   int qf = 19;             // velocity set of f
   int ratio = 0;           // density-ratio model
+  int wide = 0;            // some case needs 64-bit f offsets
   bool padded = false;     // f in the padded layout of the TMA collide
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
@@ -240,7 +242,7 @@ struct Solver {
       const int waves = -zchunk;
       int nsm = 0, occ_phi = 0, occ_col = 0;
       MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, &occ_phi, &occ_col));
+      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, wide, &occ_phi, &occ_col));
       if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
         return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
       grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
@@ -315,8 +317,14 @@ struct Solver {
     padded = n == 1 && qf == 19 && !ratio && gmode == mcb::kGEquil &&
              cs[0].nx % (gxe / 2) == 0 &&
              cs[0].variant == mcb::kTmaVariant && encode_fn() != nullptr;
+    // 32-bit f offsets need qf * cells < 2^31 in every case; larger cases run the 32x8
+    // tile with 64-bit offsets. MCB_WIDE_OFFSETS=1 forces those on any size (the tests
+    // compare the two).
+    const char* force_wide = std::getenv("MCB_WIDE_OFFSETS");
+    wide = max_cells * qf >= (1LL << 31) || (force_wide && force_wide[0] == '1');
+    if (wide) padded = false;
     if (padded) variant = mcb::kTmaVariant;
-    else if (variant == mcb::kTmaVariant || qf == 27 || ratio) variant = 0;  // the 32x8 tile
+    else if (variant == mcb::kTmaVariant || qf == 27 || ratio || wide) variant = 0;
     for (auto& d : cases) {
       if (padded) {
         d.fgx = gxe;
@@ -488,6 +496,7 @@ struct Solver {
     a.err = err;
     a.qf = qf;
     a.ratio = ratio;
+    a.wide = wide;
     a.f_in = f[parity];
     a.f_out = f[parity ^ 1];
     a.g_in = g[parity];

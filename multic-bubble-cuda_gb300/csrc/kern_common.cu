@@ -24,12 +24,12 @@ cudaError_t launch_collide_bf16(int variant, int gmode, const StepArgs& a, const
                                cudaStream_t s);
 cudaError_t prepare_tma_bf16();
 size_t tma_smem_bf16();
-cudaError_t occupancy_f32(int variant, int gmode, int qf, int ratio, int* phi_blocks,
-                          int* collide_blocks);
-cudaError_t occupancy_f16(int variant, int gmode, int qf, int ratio, int* phi_blocks,
-                          int* collide_blocks);
-cudaError_t occupancy_bf16(int variant, int gmode, int qf, int ratio, int* phi_blocks,
-                          int* collide_blocks);
+cudaError_t occupancy_f32(int variant, int gmode, int qf, int ratio, int wide,
+                          int* phi_blocks, int* collide_blocks);
+cudaError_t occupancy_f16(int variant, int gmode, int qf, int ratio, int wide,
+                          int* phi_blocks, int* collide_blocks);
+cudaError_t occupancy_bf16(int variant, int gmode, int qf, int ratio, int wide,
+                          int* phi_blocks, int* collide_blocks);
 cudaError_t launch_init_f32(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_f16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_init_bf16(const InitArgs& a, int nx, int ny, int nz, cudaStream_t s);
@@ -236,12 +236,12 @@ size_t tma_smem_bytes(int storage) {
   }
 }
 
-cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int* phi_blocks,
-                      int* collide_blocks) {
+cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int wide,
+                      int* phi_blocks, int* collide_blocks) {
   switch (storage) {
-    case kStF32: return occupancy_f32(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
-    case kStF16: return occupancy_f16(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
-    case kStBF16: return occupancy_bf16(variant, gmode, qf, ratio, phi_blocks, collide_blocks);
+    case kStF32: return occupancy_f32(variant, gmode, qf, ratio, wide, phi_blocks, collide_blocks);
+    case kStF16: return occupancy_f16(variant, gmode, qf, ratio, wide, phi_blocks, collide_blocks);
+    case kStBF16: return occupancy_bf16(variant, gmode, qf, ratio, wide, phi_blocks, collide_blocks);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -37,6 +37,7 @@
 #include <cuda_fp16.h>
 
 #include <cfloat>
+#include <type_traits>
 #include <cstring>
 
 #include "lattice.h"
@@ -569,7 +570,10 @@ __device__ __forceinline__ void f_ghosts(FT* f, long long fn, int x, int y, int 
 
 // QF: velocity set of f (19 or 27); g and the phi stencils are D3Q19 either way.
 // kRatio: the density-ratio model (f carries p* = p / (rho cs^2); see DensityRatio below).
-template <class S, int GM, int BX, int BY, bool kTma = false, int QF = kQ, bool kRatio = false>
+// kWide: 64-bit f offsets, for cases with QF * ncell >= 2^31; otherwise the offsets
+// l * ncell + cell are 32-bit signed integers (measured 9-12 % fewer instructions).
+template <class S, int GM, int BX, int BY, bool kTma = false, int QF = kQ, bool kRatio = false,
+          bool kWide = false>
 __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t,
                                                 TmaPipe* pipe = nullptr) {
   static_assert((QF == kQ && !kRatio) || !kTma, "the TMA collide is D3Q19, density-matched");
@@ -590,7 +594,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + BX * ty;
   const int x = t.xt + tx, y = t.yt + ty;
   const bool active = x < nx && y < ny;
-  const long long n = t.ncell;
+  using IT = typename std::conditional<kWide, long long, int>::type;
+  const IT n = static_cast<IT>(t.ncell);
+  const long long ng = t.ncell;  // g offsets stay 64-bit (measured: 32-bit ones spill in BGK)
 
   const CaseDesc* cd = a.cases + t.ci;
   const float omega = __ldg(&cd->omega), omega_g = __ldg(&cd->omega_g);
@@ -766,11 +772,14 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         constexpr int O = opp(L);
         const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
         if (bounce) {
-          fr[L] = S::fload(fin + O * n + idx);
+          // 32-bit: one signed offset; 64-bit: the base pointer first (cheaper there).
+          if constexpr (kWide) fr[L] = S::fload(fin + O * n + idx);
+          else fr[L] = S::fload(fin + (O * n + idx));
         } else {
           const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
                         src_of<cx(L)>(xm, x, xp);
-          fr[L] = S::fload(fin + L * n + s);
+          if constexpr (kWide) fr[L] = S::fload(fin + L * n + s);
+          else fr[L] = S::fload(fin + (L * n + s));
         }
       });
     }
@@ -788,7 +797,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       } else {
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
-          gout[(L - 1) * n + idx] = S::template g_shell<L>(pc);
+          gout[(L - 1) * ng + idx] = S::template g_shell<L>(pc);
         });
         rest_out[idx] = S::rest_shell(pc);
       }
@@ -980,12 +989,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
         int gi;
         if (bounce) {
-          gi = S::template g_dec<O>(S::gload(gin + (O - 1) * n + idx), pself);
+          gi = S::template g_dec<O>(S::gload(gin + (O - 1) * ng + idx), pself);
         } else {
           const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
                         src_of<cx(L)>(xm, x, xp);
           const int ps = S::kDev ? __ldg(pprev + s) : 0;
-          gi = S::template g_dec<L>(S::gload(gin + (L - 1) * n + s), ps);
+          gi = S::template g_dec<L>(S::gload(gin + (L - 1) * ng + s), ps);
         }
         const float gf = __int2float_rn(gi) * kInvQ30;
         go[L] = gf + omega_g * (go[L] - gf);
@@ -1005,7 +1014,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
         int q;
-        gout[(L - 1) * n + idx] = S::template g_put<L>(go[L], sp, q);
+        gout[(L - 1) * ng + idx] = S::template g_put<L>(go[L], sp, q);
         sumq += q;
       });
       rest_out[idx] = S::rest_store(pc, sumq);
@@ -1027,6 +1036,13 @@ __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     k_collide(const StepArgs a) {
   for_each_segment<BX, BY, true>(a,
                                  [&](const Tile& t) { collide_segment<S, GM, BX, BY>(a, t); });
+}
+
+// Cases of 2^31 / 19 cells or more: 64-bit f offsets, 32x8 tiles.
+template <class S, int GM>
+__global__ void __launch_bounds__(256, kCollideWarpsPerSM / 8) k_collide_wide(const StepArgs a) {
+  for_each_segment<32, 8, true>(
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ, false, true>(a, t); });
 }
 
 // The TMA variant: 32x8 tiles, f staged through shared memory (one case, (P, J) records).
@@ -1052,18 +1068,18 @@ __global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kT
 }
 
 // D3Q27 f: 32x8 tiles, two blocks of eight warps per SM (27 populations in flight).
-template <class S, int GM>
+template <class S, int GM, bool kWide>
 __global__ void __launch_bounds__(256, 2) k_collide27(const StepArgs a) {
   for_each_segment<32, 8, true>(
-      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27>(a, t); });
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27, false, kWide>(a, t); });
 }
 
 // Density-ratio model: 32x8 tiles; two blocks per SM for D3Q27 f, three for D3Q19.
-template <class S, int GM, int QF>
+template <class S, int GM, int QF, bool kWide>
 __global__ void __launch_bounds__(256, QF == kQ27 ? 2 : kCollideWarpsPerSM / 8)
     k_collide_ratio(const StepArgs a) {
   for_each_segment<32, 8, true>(
-      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, QF, true>(a, t); });
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, QF, true, kWide>(a, t); });
 }
 
 // ------------------------------------------------------------------ k_init: fields --
@@ -1203,22 +1219,30 @@ const void* collide_kernel(int variant, dim3* block) {
   }
 }
 
-template <class S, int GM>
-const void* collide_32x8_kernel(int qf, bool ratio) {
+template <class S, int GM, bool kWide>
+const void* collide_32x8_of(int qf, bool ratio) {
   if (ratio) {
-    return qf == kQ27 ? reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ27>)
-                      : reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ>);
+    return qf == kQ27 ? reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ27, kWide>)
+                      : reinterpret_cast<const void*>(k_collide_ratio<S, GM, kQ, kWide>);
   }
-  return reinterpret_cast<const void*>(k_collide27<S, GM>);
+  if (qf == kQ27) return reinterpret_cast<const void*>(k_collide27<S, GM, kWide>);
+  return kWide ? reinterpret_cast<const void*>(k_collide_wide<S, GM>) : nullptr;
 }
 
-// The 32x8 collide kernels outside the tile variants: D3Q27 f and the density-ratio model.
+template <class S, int GM>
+const void* collide_32x8_kernel(int qf, bool ratio, bool wide) {
+  return wide ? collide_32x8_of<S, GM, true>(qf, ratio)
+              : collide_32x8_of<S, GM, false>(qf, ratio);
+}
+
+// The 32x8 collide kernels outside the tile variants: D3Q27 f, the density-ratio model and
+// cases that need 64-bit f offsets.
 template <class S>
-const void* collide27_kernel(int gmode, int qf = kQ27, bool ratio = false) {
+const void* collide27_kernel(int gmode, int qf, bool ratio, bool wide) {
   switch (gmode) {
-    case kGPop: return collide_32x8_kernel<S, kGPop>(qf, ratio);
-    case kGBgk: return collide_32x8_kernel<S, kGBgk>(qf, ratio);
-    case kGEquil: return collide_32x8_kernel<S, kGEquil>(qf, ratio);
+    case kGPop: return collide_32x8_kernel<S, kGPop>(qf, ratio, wide);
+    case kGBgk: return collide_32x8_kernel<S, kGBgk>(qf, ratio, wide);
+    case kGEquil: return collide_32x8_kernel<S, kGEquil>(qf, ratio, wide);
     default: return nullptr;
   }
 }
@@ -1258,16 +1282,16 @@ cudaError_t prepare_tma_kernel() {
 
 // Resident blocks per SM of the phi and collide kernels of a variant.
 template <class S>
-cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int* phi_blocks,
+cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int wide, int* phi_blocks,
                          int* collide_blocks) {
-  if (qf == kQ27 || ratio) {
+  if (qf == kQ27 || ratio || wide) {
     dim3 bp;
     const void* fp = phi_kernel<S>(0, gmode == kGEquil, &bp);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        collide_blocks, collide27_kernel<S>(gmode, qf, ratio != 0), 256, 0);
+        collide_blocks, collide27_kernel<S>(gmode, qf, ratio != 0, wide != 0), 256, 0);
   }
   if (variant == kTmaVariant) {
     if (gmode != kGEquil) return cudaErrorInvalidValue;
@@ -1311,18 +1335,18 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
                                       const void* tmap, cudaStream_t s) {                  \
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
-    if (a.qf == kQ27 || a.ratio)                                                           \
-      return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0), a.grid_collide,     \
-                       dim3(32, 8), a, s);                                                 \
+    if (a.qf == kQ27 || a.ratio || a.wide)                                                 \
+      return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0, a.wide != 0),        \
+                       a.grid_collide, dim3(32, 8), a, s);                                 \
     dim3 block;                                                                            \
     const void* fn = collide_kernel_gm<S>(variant, gmode, &block);                         \
     return launch_on(fn, a.grid_collide, block, a, s);                                     \
   }                                                                                        \
   cudaError_t prepare_tma_##suffix() { return prepare_tma_kernel<S>(); }                   \
   size_t tma_smem_##suffix() { return TmaBox<typename S::FT>::kSmem; }                     \
-  cudaError_t occupancy_##suffix(int variant, int gmode, int qf, int ratio,                \
+  cudaError_t occupancy_##suffix(int variant, int gmode, int qf, int ratio, int wide,      \
                                  int* phi_blocks, int* collide_blocks) {                   \
-    return occupancy_of<S>(variant, gmode, qf, ratio, phi_blocks, collide_blocks);         \
+    return occupancy_of<S>(variant, gmode, qf, ratio, wide, phi_blocks, collide_blocks);   \
   }                                                                                        \
   cudaError_t launch_init_##suffix(const InitArgs& a, int nx, int ny, int nz,              \
                                    cudaStream_t s) {                                       \

@@ -65,6 +65,7 @@ struct StepArgs {
   int* err;            // set to a nonzero code when a bounded wait of a kernel gives up
   int qf;              // velocity set of f: 19 or 27 (every case of a launch)
   int ratio;           // 1: the density-ratio model (every case of a launch)
+  int wide;            // 1: some case has QF * ncell >= 2^31 (64-bit f offsets)
   const void* f_in;   // 19 arrays per case
   void* f_out;
   const void* g_in;   // 18 moving g arrays per case (l = 1..18)
@@ -137,8 +138,8 @@ cudaError_t prepare_tma(int storage);
 // Dynamic shared memory of the TMA collide kernel for a storage.
 size_t tma_smem_bytes(int storage);
 // Resident blocks per SM of the phi and collide kernels of a tile variant.
-cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int* phi_blocks,
-                      int* collide_blocks);
+cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, int wide,
+                      int* phi_blocks, int* collide_blocks);
 cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);
 cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s);

@@ -250,6 +250,22 @@ def test_work_splits_agree_bitwise_with_equilibrium_g(storage):
                 assert np.array_equal(r[k], base[k]), (v, zc, k)
 
 
+@pytest.mark.parametrize("velocity_set,ratio,tau_g", [(19, 1.0, 1.0), (19, 1.0, 0.8),
+                                                     (27, 1.0, 1.0), (19, 10.0, 1.0)])
+def test_64bit_population_offsets_agree_bitwise(monkeypatch, velocity_set, ratio, tau_g):
+    """Cases of 2^31 / Q cells or more address f with 64-bit offsets; every other case with
+    32-bit ones. MCB_WIDE_OFFSETS=1 forces the 64-bit kernels on a small case: the fields
+    must not change."""
+    cfg, phi, u = small_case(mcb.BC_WALLS_Z, tau_g=tau_g, gravity=1e-4, noise=1e-3)
+    cfg.velocity_set = velocity_set
+    cfg.rho_in = ratio
+    base = gpu_run(cfg, phi, u, steps=23)
+    monkeypatch.setenv("MCB_WIDE_OFFSETS", "1")
+    wide = gpu_run(cfg, phi, u, steps=23)
+    for k in FIELDS:
+        assert np.array_equal(wide[k], base[k]), k
+
+
 def test_steps_split_across_calls_agree_bitwise():
     cfg, phi, u = small_case(mcb.BC_PERIODIC, tau_g=0.8, noise=1e-3)
     one = gpu_run(cfg, phi, u, steps=50)
