@@ -82,8 +82,9 @@ typedef struct mcb_config {
     int   variant;      /* kernel tile variant, -1 = default (see mcb_variant_count) */
     int   zchunk;       /* work split: > 0 fixed chunks of zchunk z planes per block;
                            -w (w <= 16) balanced over w waves of resident blocks, each
-                           block taking an equal run of planes; 0 = default (balanced
-                           with (phi, J) records, fixed chunks otherwise) */
+                           block taking an equal run of planes; 0 = default (one wave of
+                           equal chunks when one case's tile columns fit in it, else
+                           32-plane chunks) */
     int   use_graph;    /* 1 = replay updates from a CUDA graph, 0 = plain launches */
     int   g_mode;       /* how g crosses between updates:
                            MCB_G_AUTO: with tau_g = 1 every post-collision g population is

@@ -51,9 +51,8 @@ int fail(int code, const char* fmt, ...) {
     if (r_ != MCB_OK) return r_; \
   } while (0)
 
-// Balanced work decomposition: resident waves of equal-work blocks per kernel. One wave
-// has no tail: every block of the launch finishes at the same time.
-constexpr int kDefaultWaves = 1;
+// Balanced work decomposition (zchunk = -w): w resident waves of equal-work blocks per
+// kernel.
 constexpr int kMaxWaves = 16;
 constexpr int kMinCollidePlanes = 8;
 
@@ -196,10 +195,7 @@ struct Solver {
   //   zchunk_req > 0: fixed chunks of that many planes, one block each;
   //   zchunk_req < 0: balanced ranges, -zchunk_req resident waves of equal-work blocks
   //   per kernel;
-  //   zchunk_req == 0: balanced over kDefaultWaves with equilibrium g storage; fixed
-  //   chunks otherwise (measured on GB300 at 128x128x256: balanced ranges are 2 % faster
-  //   with (P, J) records at FP16 and equal at FP32, while the stored-population phi
-  //   kernel is 25 % slower with them than with 16-plane chunks).
+  //   zchunk_req == 0: fixed chunks chosen below.
   int build_tiles() {
     const mcb::Variant v = mcb::kVariants[variant];
     long long plane_total = 0;
@@ -211,7 +207,12 @@ struct Solver {
       if (plane_total > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tile planes");
     }
     planes = static_cast<int>(plane_total);
-    balanced = zchunk_req < 0 || (zchunk_req == 0 && gmode == mcb::kGEquil);
+    balanced = zchunk_req < 0;
+    int nsm = 0, occ_phi = 0, occ_col = 0;
+    MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, wide, &occ_phi, &occ_col));
+    if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
+      return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
     auto tiles_for = [&](int zc) {
       long long total = 0;
       for (auto& d : cases)
@@ -220,11 +221,25 @@ struct Solver {
     };
     int zc = zchunk_req;
     if (zc <= 0) {
-      // Fixed-chunk default: at least three waves of two blocks per SM on 152 SMs; longer
-      // chunks amortise the halo planes of the march (measured best: 16 planes at
-      // 128x128x256).
-      zc = 32;
-      while (zc > 4 && tiles_for(zc) < 3LL * 2 * 152) zc /= 2;
+      // Default split, from sweeps on GB300: when one case's tile columns fit in one
+      // resident wave of collide blocks, cut every column into the same number of chunks so
+      // that the whole case is one wave whose blocks march neighbouring columns in step
+      // (128x128x256: 37 planes, 2 % faster than 16-plane chunks, 2.4 % faster than
+      // balanced runs at FP32). Otherwise 32-plane chunks (512^3: 13 % faster than balanced
+      // runs, 2.5 % faster than 16), keeping at least 8 planes per chunk.
+      const long long wave = 1LL * occ_col * nsm;
+      long long cols = 0;
+      int nzmax = 1;
+      for (auto& d : cases) {
+        cols += static_cast<long long>(d.tiles_x) * d.tiles_y;
+        nzmax = std::max(nzmax, d.nz);
+      }
+      if (cases.size() == 1 && cols <= wave) {
+        const long long m = std::max<long long>(1, std::min<long long>(wave / cols, nzmax / 8));
+        zc = static_cast<int>((nzmax + m - 1) / m);
+      } else {
+        zc = 32;
+      }
     }
     const long long tile0_total = tiles_for(zc);
     if (tile0_total > 0x7fffffffLL)
@@ -237,14 +252,9 @@ struct Solver {
       tile0 += static_cast<long long>(d.tiles_x) * d.tiles_y * d.tiles_z;
     }
     ntiles = static_cast<int>(tile0);
-    zchunk = balanced ? (zchunk_req < 0 ? zchunk_req : -kDefaultWaves) : zc;
+    zchunk = balanced ? zchunk_req : zc;
     if (balanced) {
       const int waves = -zchunk;
-      int nsm = 0, occ_phi = 0, occ_col = 0;
-      MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-      MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, wide, &occ_phi, &occ_col));
-      if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
-        return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
       grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
       // A collide piece re-reads four phi planes and recomputes two normal planes before
       // its first plane: give each block at least kMinCollidePlanes.
