@@ -214,9 +214,9 @@ struct Tile {
 };
 
 // The tile-planes [p0, p1) of this block.
-__device__ __forceinline__ int2 block_range(const StepArgs& a) {
+__device__ __forceinline__ int2 block_range(const StepArgs& a, bool balanced) {
   const int b = static_cast<int>(blockIdx.x);
-  if (a.balanced) {
+  if (balanced) {
     const long long P = a.planes, G = gridDim.x;
     return make_int2(static_cast<int>(b * P / G), static_cast<int>((b + 1) * P / G));
   }
@@ -261,8 +261,9 @@ __device__ __forceinline__ Tile segment_tile(const StepArgs& a, int p, int p1) {
 // Runs body(tile) over the column pieces of this block's range. sync: a block barrier
 // between pieces, for kernels whose pieces reuse shared memory.
 template <int BX, int BY, bool kSync, class Body>
-__device__ __forceinline__ void for_each_segment(const StepArgs& a, Body&& body) {
-  const int2 r = block_range(a);
+__device__ __forceinline__ void for_each_segment(const StepArgs& a, Body&& body,
+                                                 bool balanced) {
+  const int2 r = block_range(a, balanced);
   for (int p = r.x; p < r.y;) {
     const Tile t = segment_tile<BX, BY>(a, p, r.y);
     if (kSync && p != r.x) __syncthreads();
@@ -354,7 +355,8 @@ __device__ __forceinline__ void phi_segment(const StepArgs& a, const Tile& t) {
 template <class S, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY))
     k_phi(const StepArgs a) {
-  for_each_segment<BX, BY, false>(a, [&](const Tile& t) { phi_segment<S, BX, BY>(a, t); });
+  for_each_segment<BX, BY, false>(
+      a, [&](const Tile& t) { phi_segment<S, BX, BY>(a, t); }, a.balanced != 0);
 }
 
 // ------------------------------------- k_phi_eq: g -> phi when g is stored as (phi, J) --
@@ -444,7 +446,8 @@ __device__ __forceinline__ void phi_eq_segment(const StepArgs& a, const Tile& t)
 
 template <class S, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY, 32 * 32 / (BX * BY)) k_phi_eq(const StepArgs a) {
-  for_each_segment<BX, BY, false>(a, [&](const Tile& t) { phi_eq_segment<S, BX, BY>(a, t); });
+  for_each_segment<BX, BY, false>(
+      a, [&](const Tile& t) { phi_eq_segment<S, BX, BY>(a, t); }, a.phi_balanced != 0);
 }
 
 // ------------------------------------------- TMA staging of f for the collide kernel --
@@ -1035,14 +1038,14 @@ template <class S, int GM, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY, kCollideWarpsPerSM * 32 / (BX * BY))
     k_collide(const StepArgs a) {
   for_each_segment<BX, BY, true>(a,
-                                 [&](const Tile& t) { collide_segment<S, GM, BX, BY>(a, t); });
+                                 [&](const Tile& t) { collide_segment<S, GM, BX, BY>(a, t); }, a.balanced != 0);
 }
 
 // Cases of 2^31 / 19 cells or more: 64-bit f offsets, 32x8 tiles.
 template <class S, int GM>
 __global__ void __launch_bounds__(256, kCollideWarpsPerSM / 8) k_collide_wide(const StepArgs a) {
   for_each_segment<32, 8, true>(
-      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ, false, true>(a, t); });
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ, false, true>(a, t); }, a.balanced != 0);
 }
 
 // The TMA variant: 32x8 tiles, f staged through shared memory (one case, (P, J) records).
@@ -1064,14 +1067,14 @@ __global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kT
     if (pipe.failed) return;
     collide_segment<S, kGEquil, kTmaBX, kTmaBY, true>(a, t, &pipe);
     pipe.it += static_cast<unsigned>(t.ze - t.zb);
-  });
+  }, a.balanced != 0);
 }
 
 // D3Q27 f: 32x8 tiles, two blocks of eight warps per SM (27 populations in flight).
 template <class S, int GM, bool kWide>
 __global__ void __launch_bounds__(256, 2) k_collide27(const StepArgs a) {
   for_each_segment<32, 8, true>(
-      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27, false, kWide>(a, t); });
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27, false, kWide>(a, t); }, a.balanced != 0);
 }
 
 // Density-ratio model: 32x8 tiles; two blocks per SM for D3Q27 f, three for D3Q19.
@@ -1079,7 +1082,7 @@ template <class S, int GM, int QF, bool kWide>
 __global__ void __launch_bounds__(256, QF == kQ27 ? 2 : kCollideWarpsPerSM / 8)
     k_collide_ratio(const StepArgs a) {
   for_each_segment<32, 8, true>(
-      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, QF, true, kWide>(a, t); });
+      a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, QF, true, kWide>(a, t); }, a.balanced != 0);
 }
 
 // ------------------------------------------------------------------ k_init: fields --

@@ -59,6 +59,7 @@ struct StepArgs {
   int ncases;
   int ntiles;
   int balanced;
+  int phi_balanced;    // the record phi kernel always takes balanced ranges
   int planes;          // P, tile-planes of all cases
   int grid_phi;        // blocks of the phi kernel
   int grid_collide;    // blocks of the collide kernel
