@@ -139,7 +139,7 @@ struct Solver {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_steps = 16;
   int ntiles = 0, zchunk = 16;
-  int balanced = 1, planes = 0, grid_phi = 0, grid_collide = 0;
+  int balanced = 1, phi_balanced = 0, planes = 0, grid_phi = 0, grid_collide = 0;
   int parity = 0, first = 1, latest_p = 1;
   long long update = -1;
   std::vector<char> fields_set;
@@ -253,6 +253,7 @@ struct Solver {
     }
     ntiles = static_cast<int>(tile0);
     zchunk = balanced ? zchunk_req : zc;
+    phi_balanced = 0;
     if (balanced) {
       const int waves = -zchunk;
       grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
@@ -262,10 +263,12 @@ struct Solver {
           std::max(1, planes / kMinCollidePlanes), 1LL * occ_col * nsm * waves));
     } else {
       grid_phi = grid_collide = ntiles;
-      // The record phi kernel has no halo to prime: one resident wave of equal runs, which
-      // fills the GPU whatever the collide chunks (measured 56 us against 59 at
-      // 128x128x256, and 57 against 87 with the D3Q27 chunks).
-      if (gmode == mcb::kGEquil)
+      // When the collide chunks leave part of a phi wave idle, the record phi kernel (no
+      // halo to prime) takes one resident wave of equal runs instead: 128x128x256 57 us
+      // against 59, with the D3Q27 chunks 57 against 87. Larger cases keep the chunks
+      // (512^3: 1.47 ms against 1.74 balanced).
+      phi_balanced = gmode == mcb::kGEquil && ntiles < 1LL * occ_phi * nsm;
+      if (phi_balanced)
         grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm));
     }
     drop_graphs();
@@ -505,7 +508,7 @@ struct Solver {
     a.ncases = static_cast<int>(cases.size());
     a.ntiles = ntiles;
     a.balanced = balanced;
-    a.phi_balanced = balanced || gmode == mcb::kGEquil;
+    a.phi_balanced = balanced || phi_balanced;
     a.planes = planes;
     a.grid_phi = grid_phi;
     a.grid_collide = grid_collide;
