@@ -859,16 +859,19 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
     float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
     float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
-    static_for<0, QF>([&](auto LC) {
-      constexpr int L = decltype(LC)::value;
-      const float v = f[L];
-      rho += v;
-      if constexpr (cx(L) != 0) { jx += cx(L) * v; sxx += v; }
-      if constexpr (cy(L) != 0) { jy += cy(L) * v; syy += v; }
-      if constexpr (cz(L) != 0) { jz += cz(L) * v; szz += v; }
-      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * v;
-      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
-      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
+    // Opposite pairs (L, L+1): their sum carries the even moments, their difference the
+    // odd ones.
+    rho += f[0];
+    static_for<0, (QF - 1) / 2>([&](auto KC) {
+      constexpr int L = 2 * decltype(KC)::value + 1;
+      const float sa = f[L] + f[L + 1], da = f[L] - f[L + 1];
+      rho += sa;
+      if constexpr (cx(L) != 0) { jx += cx(L) * da; sxx += sa; }
+      if constexpr (cy(L) != 0) { jy += cy(L) * da; syy += sa; }
+      if constexpr (cz(L) != 0) { jz += cz(L) * da; szz += sa; }
+      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * sa;
+      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * sa;
+      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * sa;
     });
     float ux, uy, uz, pxx, pyy, pzz, pxy, pxz, pyz, inv_rp = 0.f, rp = 1.f;
     if constexpr (kRatio) {
@@ -949,16 +952,21 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       if constexpr (cx(L) * cy(L) != 0) qp += (2 * cx(L) * cy(L)) * pxy;
       if constexpr (cx(L) * cz(L) != 0) qp += (2 * cx(L) * cz(L)) * pxz;
       if constexpr (cy(L) * cz(L) != 0) qp += (2 * cy(L) * cz(L)) * pyz;
-      const float q = om * qp + fshift;
-      const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
-      const float rf = 1.5f * cF;
       if constexpr (kRatio) {
+        const float q = om * qp;
+        const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
         const float fe = cf * cF;
         fo[L] = W * (e0 + q + (e1 + fe));
         fo[O] = W * (e0 + q - (e1 + fe));
       } else {
-        fo[L] = W * ((e0 + e1) * (R + rf) + q);
-        fo[O] = W * ((e0 - e1) * (R - rf) + q);
+        // The weight folded into each term: W e0 = W base + (9/2 W) cu^2, W e1 = 3 W cu,
+        // W q = (W om) qp + W fshift.
+        const float we0 = (4.5f * W) * cu * cu + W * base;
+        const float we1 = (3.0f * W) * cu;
+        const float wq = (W * om) * qp + W * fshift;
+        const float rf = 1.5f * cF;
+        fo[L] = (we0 + we1) * (R + rf) + wq;
+        fo[O] = (we0 - we1) * (R - rf) + wq;
       }
       if constexpr (L < kQ) {
         constexpr float WG = wf(L);  // g is D3Q19
