@@ -952,21 +952,19 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       if constexpr (cx(L) * cy(L) != 0) qp += (2 * cx(L) * cy(L)) * pxy;
       if constexpr (cx(L) * cz(L) != 0) qp += (2 * cx(L) * cz(L)) * pxz;
       if constexpr (cy(L) * cz(L) != 0) qp += (2 * cy(L) * cz(L)) * pyz;
+      const float q = om * qp + fshift;
+      const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
       if constexpr (kRatio) {
-        const float q = om * qp;
-        const float e0 = base + 4.5f * cu * cu, e1 = 3.0f * cu;
         const float fe = cf * cF;
         fo[L] = W * (e0 + q + (e1 + fe));
         fo[O] = W * (e0 + q - (e1 + fe));
       } else {
-        // The weight folded into each term: W e0 = W base + (9/2 W) cu^2, W e1 = 3 W cu,
-        // W q = (W om) qp + W fshift.
-        const float we0 = (4.5f * W) * cu * cu + W * base;
-        const float we1 = (3.0f * W) * cu;
-        const float wq = (W * om) * qp + W * fshift;
+        // The weight stays outside: folding it into the terms (W base + ...) changed the
+        // rounding of the small non-equilibrium part enough to shift the D3Q27 shear-wave
+        // viscosity by 4 %.
         const float rf = 1.5f * cF;
-        fo[L] = (we0 + we1) * (R + rf) + wq;
-        fo[O] = (we0 - we1) * (R - rf) + wq;
+        fo[L] = W * ((e0 + e1) * (R + rf) + q);
+        fo[O] = W * ((e0 - e1) * (R - rf) + q);
       }
       if constexpr (L < kQ) {
         constexpr float WG = wf(L);  // g is D3Q19
