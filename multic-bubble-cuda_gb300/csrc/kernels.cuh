@@ -859,19 +859,16 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
     float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
     float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
-    // Opposite pairs (L, L+1): their sum carries the even moments, their difference the
-    // odd ones.
-    rho += f[0];
-    static_for<0, (QF - 1) / 2>([&](auto KC) {
-      constexpr int L = 2 * decltype(KC)::value + 1;
-      const float sa = f[L] + f[L + 1], da = f[L] - f[L + 1];
-      rho += sa;
-      if constexpr (cx(L) != 0) { jx += cx(L) * da; sxx += sa; }
-      if constexpr (cy(L) != 0) { jy += cy(L) * da; syy += sa; }
-      if constexpr (cz(L) != 0) { jz += cz(L) * da; szz += sa; }
-      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * sa;
-      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * sa;
-      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * sa;
+    static_for<0, QF>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      const float v = f[L];
+      rho += v;
+      if constexpr (cx(L) != 0) { jx += cx(L) * v; sxx += v; }
+      if constexpr (cy(L) != 0) { jy += cy(L) * v; syy += v; }
+      if constexpr (cz(L) != 0) { jz += cz(L) * v; szz += v; }
+      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * v;
+      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
+      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
     });
     float ux, uy, uz, pxx, pyy, pzz, pxy, pxz, pyz, inv_rp = 0.f, rp = 1.f;
     if constexpr (kRatio) {
@@ -959,9 +956,10 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         fo[L] = W * (e0 + q + (e1 + fe));
         fo[O] = W * (e0 + q - (e1 + fe));
       } else {
-        // The weight stays outside: folding it into the terms (W base + ...) changed the
-        // rounding of the small non-equilibrium part enough to shift the D3Q27 shear-wave
-        // viscosity by 4 %.
+        // The weight stays outside the bracket. Folding it into the terms (W base + ...)
+        // changed the rounding of the small non-equilibrium part enough to shift the D3Q27
+        // shear-wave viscosity by 4 %; summing opposite pairs first in the moments moved
+        // the 2000-update static bubble 1.4e-4 from the FP64 oracle (1.5 % faster).
         const float rf = 1.5f * cF;
         fo[L] = W * ((e0 + e1) * (R + rf) + q);
         fo[O] = W * ((e0 - e1) * (R - rf) + q);
