@@ -228,9 +228,10 @@ int  mcb_step_profiled(mcb_handle* h, int nsteps, float* total_ms, float* phi_ms
 int  mcb_variant_count(void);
 int  mcb_variant_shape(int variant, int* bx, int* by);
 
-/* Times every tile variant and z chunk on a copy of the handle's state for nsteps
- * updates each. Keeps the fastest variant in the handle, and reports it and its MLUPS.
- * The handle's fields are restored afterwards. */
+/* Times every tile variant and work split (the mcb_config.zchunk values 0, -1..-4, 8, 16,
+ * 32) on a copy of the handle's state for nsteps updates each. Keeps the fastest in the
+ * handle and reports it (best_zchunk 0: the default split) and its MLUPS. The handle's
+ * fields are restored afterwards. */
 int  mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
                   double* best_mlups);
 

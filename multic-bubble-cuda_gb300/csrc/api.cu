@@ -1157,8 +1157,8 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   int rc = snapshot(false);
   double best = -1.0;
   int bv = save_variant, bz = s.zchunk;
-  // Balanced ranges of 1..4 resident waves, then fixed chunks.
-  const int zc_list[] = {-1, -2, -3, -4, 8, 16, 32};
+  // The default split, balanced ranges of 1..4 resident waves, then fixed chunks.
+  const int zc_list[] = {0, -1, -2, -3, -4, 8, 16, 32};
   for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
     // The f layout is fixed at creation: the TMA variant alone on the padded layout, the
     // plain tiles otherwise.

@@ -380,8 +380,8 @@ def test_autotune_restores_the_state():
         s.set_fields(phi, *u)
         s.step(10)
         v, zc, ml = s.autotune(nsteps=4)
-        # zc > 0: fixed chunks; zc < 0: balanced over -zc waves.
-        assert 0 <= v < mcb.lib().mcb_variant_count() and -16 <= zc != 0 and ml > 0
+        # zc > 0: fixed chunks; zc < 0: balanced over -zc waves; 0: the default split.
+        assert 0 <= v < mcb.lib().mcb_variant_count() and -16 <= zc <= 64 and ml > 0
         s.step(10)
         for k in FIELDS:
             assert np.array_equal(s.get(k).astype(np.float64), ref[k]), k
