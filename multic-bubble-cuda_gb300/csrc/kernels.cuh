@@ -8,9 +8,12 @@
 //   k_phi      pull-gathers the 19 g populations of every cell and sums them into phi.
 //              This is streamingCalc + phiCalc (src/lbm.cu:337-357, 5-26), plus the lagged
 //              shell copy of boundaryConditions (src/lbm.cu:403-425) in reference mode.
+//   k_phi_eq   the same when g is stored as one (phi, J) record per cell (full g
+//              relaxation, the default): it rebuilds the 18 pulled populations exactly.
 //   k_collide  marches a BX x BY column of cells through a z chunk. It keeps a 5-plane
-//              ring of phi (halo 2) and a 3-plane ring of normals (halo 1) in shared
-//              memory. For every cell it computes:
+//              ring of phi (halo 2) and a 4-plane ring of normals (halo 1) in shared
+//              memory, the normals computed one plane ahead so that each plane takes one
+//              block barrier. For every cell it computes:
 //                - the isotropic normals and |grad phi| (gradCalc, src/lbm.cu:34-72);
 //                - the curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125);
 //                - the moments (momentiCalc, src/lbm.cu:133-225);
@@ -22,9 +25,10 @@
 //              shell cells write the rest-equilibrium inflow of fgBoundary
 //              (src/lbm.cu:365-401).
 //
-// HBM traffic per lattice update: f and g are read once and written once, plus 8 bytes
-// of phi. Nothing else reaches HBM: normals, curvature, force and moments live in
-// registers and shared memory.
+// HBM traffic per lattice update: f read and written once, plus either the 16-byte record
+// written once and read once (default) or g read and written once, plus 8 bytes of phi.
+// Nothing else reaches HBM: normals, curvature, force and moments live in registers and
+// shared memory.
 //
 // phi is carried as Q2.30 fixed point. Every g collision writes the rest population as
 // the exact integer remainder. The 19 stored values of a cell therefore add up to its
@@ -589,7 +593,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   constexpr int HX = BX + 2, HY = BY + 2, HP = HX * HY;  // normals plane, halo 1
   constexpr int KPF = (PP + NT - 1) / NT;                // phi values per thread per plane
   __shared__ float sphi[5][PP];
-  __shared__ float snrm[3][4][HP];  // nx, ny, nz, |grad phi| of three planes
+  __shared__ float snrm[4][4][HP];  // nx, ny, nz, |grad phi| of four planes
 
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int nxy = nx * ny;
@@ -648,7 +652,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     const float* pm = sphi[(zp + 4) % 5];
     const float* p0 = sphi[(zp + 5) % 5];
     const float* pp = sphi[(zp + 6) % 5];
-    float(*dst)[HP] = snrm[(zp + 3) % 3];
+    float(*dst)[HP] = snrm[(zp + 4) % 4];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
     for (int i = tid; i < HP; i += NT) {
       const int hx = i % HX, hy = i / HX;
@@ -710,19 +714,23 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
   }
 
-  // Prologue: phi planes zb-2 .. zb+1, normals zb-1 and zb.
-  for (int zpl = t.zb - 2; zpl <= t.zb + 1; ++zpl) {
+  // Prologue: phi planes zb-2 .. zb+2, normals zb-1 .. zb+1. Each plane then takes one
+  // barrier: the normals of plane z+2 are computed one plane ahead, after it, into a
+  // 4-plane ring, while the collision of plane z reads planes z-1 .. z+1.
+  for (int zpl = t.zb - 2; zpl <= t.zb + 2; ++zpl) {
     issue(zpl);
     commit(zpl);
   }
-  issue(t.zb + 2);
+  issue(t.zb + 3);
   __syncthreads();
   normals(t.zb - 1);
   normals(t.zb);
+  normals(t.zb + 1);
+  __syncthreads();
 
   for (int z = t.zb; z < t.ze; ++z) {
-    commit(z + 2);
-    if (z + 3 <= t.ze + 1) issue(z + 3);
+    commit(z + 3);
+    if (z + 4 <= t.ze + 1) issue(z + 4);
 
     const int zo = z * nxy;
     const int idx = x + yo + zo;
@@ -787,8 +795,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       });
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
-    normals(z + 1);
-    __syncthreads();
+    if (z + 2 <= t.ze) normals(z + 2);
     if (!active) continue;
 
     const int pc = __ldg(pcur + idx);
@@ -817,9 +824,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
 
     // Curvature and interfacial force (curvatureCalc, src/lbm.cu:80-125). Each neighbour
     // contributes c.n, so only the components along its nonzero c are read.
-    const float(*nm)[HP] = snrm[(z + 2) % 3];
-    const float(*n0)[HP] = snrm[(z + 3) % 3];
-    const float(*np)[HP] = snrm[(z + 4) % 3];
+    const float(*nm)[HP] = snrm[(z + 3) % 4];
+    const float(*n0)[HP] = snrm[(z + 4) % 4];
+    const float(*np)[HP] = snrm[(z + 5) % 4];
     const int hc = (ty + 1) * HX + tx + 1;
     const float4 nc = make_float4(n0[0][hc], n0[1][hc], n0[2][hc], n0[3][hc]);
     float kap = 0.f;
