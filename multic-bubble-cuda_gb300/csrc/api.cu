@@ -122,6 +122,7 @@ struct Solver {
   int ratio = 0;           // density-ratio model
   int wide = 0;            // some case needs 64-bit f offsets
   bool padded = false;     // f in the padded layout of the TMA collide
+  bool push = false;       // records not stored: the collide kernel writes the next phi
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
   mcb::CaseDesc* d_cases = nullptr;
@@ -373,7 +374,10 @@ struct Solver {
       }
       MCB_CU(cudaMalloc(&p[i], cb));
     }
-    if (gmode == mcb::kGEquil)
+    // (phi, J) records: with full g relaxation every collide kernel but the TMA one writes
+    // the next phi itself; the TMA one keeps the records and the phi kernel.
+    push = gmode == mcb::kGEquil && !padded;
+    if (gmode == mcb::kGEquil && !push)
       MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * sizeof(float4)));
     MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
     MCB_CU(cudaMalloc(&stage, static_cast<size_t>(max_cells) * 4 * sizeof(float)));
@@ -524,6 +528,7 @@ struct Solver {
     a.rest_out = rest[parity ^ 1];
     a.p_prev = p[parity ^ 1];
     a.p_cur = p[parity];
+    a.p_next = push ? p[parity ^ 1] : nullptr;
     a.macros = with_macros ? macros : nullptr;
     a.j = jbuf;
     a.cells_total = cells_total;
@@ -533,11 +538,21 @@ struct Solver {
 
   // Equilibrium storage has no populations before the first collision: its first update
   // takes phi from the init and runs only the collide kernel.
-  bool skips_phi() const { return gmode == mcb::kGEquil && first; }
+  bool skips_phi() const { return gmode == mcb::kGEquil && (push || first); }
+
+  // The phi stage of an update: the phi kernel, or (push) clearing the next phi.
+  int launch_phi_stage(const mcb::StepArgs& a) {
+    if (push)
+      MCB_CU(cudaMemsetAsync(p[parity ^ 1], 0, static_cast<size_t>(cells_total) * sizeof(int),
+                             stream));
+    else if (!skips_phi())
+      MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+    return MCB_OK;
+  }
 
   int launch_update(bool with_macros) {
     const mcb::StepArgs a = args(with_macros);
-    if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+    MCB_TRY(launch_phi_stage(a));
     MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
                                stream));
     latest_p = parity;
@@ -620,7 +635,7 @@ struct Solver {
     MCB_CU(cudaEventRecord(ev0, stream));
     for (int i = 0; i < nsteps; ++i) {
       const mcb::StepArgs a = args(i == nsteps - 1);
-      if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+      MCB_TRY(launch_phi_stage(a));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 1], stream));
       MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
                                stream));
@@ -664,7 +679,7 @@ struct Solver {
     std::vector<std::pair<void*, size_t>> v;
     v.push_back({f[parity], f_bytes()});
     if (gmode == mcb::kGEquil) {
-      v.push_back({jbuf, n * sizeof(float4)});
+      if (jbuf) v.push_back({jbuf, n * sizeof(float4)});
     } else {
       v.push_back({g[parity], n * 18 * pop_bytes(storage)});
       v.push_back({rest[parity], n * sizeof(int)});
@@ -1105,7 +1120,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   const bool eq = s.gmode == mcb::kGEquil;
   const size_t fb = s.f_bytes();
   // Equilibrium storage keeps a (phi, J) record per cell in place of g and its rest.
-  const size_t gb = eq ? n * sizeof(float4) : n * 18 * pop_bytes(s.storage);
+  const size_t gb = eq ? (s.jbuf ? n * sizeof(float4) : 0) : n * 18 * pop_bytes(s.storage);
   void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
   auto free_all = [&]() {
     cudaFree(fs);
@@ -1114,7 +1129,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     cudaFree(ps);
     cudaFree(ms);
   };
-  if (cudaMalloc(&fs, fb) != cudaSuccess || cudaMalloc(&gs, gb) != cudaSuccess ||
+  if (cudaMalloc(&fs, fb) != cudaSuccess || (gb && cudaMalloc(&gs, gb) != cudaSuccess) ||
       cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 8) != cudaSuccess ||
       cudaMalloc(&ms, n * 20) != cudaSuccess) {
     free_all();
@@ -1130,14 +1145,14 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     cudaError_t e = cudaSuccess;
     if (!restore) {
       if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
-      if (e == cudaSuccess) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
+      if (e == cudaSuccess && gb) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
       if (e == cudaSuccess && !eq) e = cp(rs, s.rest[par], n * 4);
       if (e == cudaSuccess) e = cp(ps, s.p[0], n * 4);
       if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + n * 4, s.p[1], n * 4);
       if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
     } else {
       if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
-      if (e == cudaSuccess) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
+      if (e == cudaSuccess && gb) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
       if (e == cudaSuccess && !eq) e = cp(s.rest[par], rs, n * 4);
       if (e == cudaSuccess) e = cp(s.p[0], ps, n * 4);
       if (e == cudaSuccess) e = cp(s.p[1], static_cast<char*>(ps) + n * 4, n * 4);

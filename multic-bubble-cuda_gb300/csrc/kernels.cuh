@@ -647,6 +647,55 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     for (int k = 0; k < KPF; ++k)
       if (tid + k * NT < PP) d[tid + k * NT] = __int2float_rn(pre[k]) * kInvQ30;
   };
+  // kPush: the collide kernel writes the next update's phi itself. Each cell s pushes its
+  // 19 exact Q2.30 populations q_l = w_l(P_s) + rn(W_l c_l.J_s 2^30) to their consumers
+  // s + c_l (the same integers the record rebuild pulls): inside the tile through a
+  // 4-plane shared ring of integer sums (tile + halo 1), flushed to global memory with
+  // integer atomic adds once a target plane is complete. Integer sums do not depend on the
+  // order, so the result is the record rebuild's, bit for bit, with no records and no phi
+  // kernel.
+  constexpr bool kPush = EQ && !kTma;
+  __shared__ int sacc[kPush ? 4 : 1][kPush ? HP : 1];
+  int* __restrict__ pnext = kPush ? a.p_next + t.cell_off : nullptr;
+  // Global in-plane offsets of this thread's two accumulator positions (-1: none).
+  int aoff[2] = {-1, -1};
+  if constexpr (kPush) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int i = tid + k * NT;
+      if (i >= HP) continue;
+      int gx = t.xt - 1 + i % HX, gy = t.yt - 1 + i / HX;
+      if (ref) {
+        // outside the lattice, or a shell cell (its phi is the lagged copy): no target
+        if (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1) continue;
+      } else {
+        gx = wrap1(gx, nx);
+        gy = wrap1(gy, ny);
+        if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+      }
+      aoff[k] = gx + gy * nx;
+    }
+    for (int i = tid; i < 4 * HP; i += NT) (&sacc[0][0])[i] = 0;
+  }
+  // Adds the integer sums of target plane q to the next phi and clears the ring slot.
+  auto flush = [&](int q) {
+    if constexpr (kPush) {
+      int* slot = sacc[(q + 8) % 4];
+      int qz = q;
+      if (t.bc == kBcPeriodic) qz = wrap1(q, nz);
+      const bool plane_ok = ref ? (qz > 0 && qz < nz - 1) : (qz >= 0 && qz < nz);
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = tid + k * NT;
+        if (i >= HP) continue;
+        const int v = slot[i];
+        slot[i] = 0;
+        if (v != 0 && plane_ok && aoff[k] >= 0)
+          atomicAdd(pnext + aoff[k] + static_cast<long long>(qz) * nxy, v);
+      }
+    }
+  };
+
   // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72).
   auto normals = [&](int zp) {
     const float* pm = sphi[(zp + 4) % 5];
@@ -713,6 +762,28 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       }
     }
   }
+
+  // Pushes the populations of source cell (x, y, z), phi P and flux (jx, jy, jz), into the
+  // shared ring: q_l to target plane z + cz(l), the rest part and populations bounced at a
+  // z wall to the cell itself.
+  auto push = [&](int z, int P, float jx, float jy, float jz) {
+    if constexpr (kPush) {
+      const int o = (ty + 1) * HX + tx + 1;
+      const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+      int self = wsplit_rest(P);
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        const int q = wsplit<L>(P) + qj<L>(jx, jy, jz);
+        const bool bounce = (cz(L) == -1) ? blo : ((cz(L) == 1) ? bhi : false);
+        if (bounce) {
+          self += q;
+        } else {
+          atomicAdd(&sacc[(z + cz(L) + 8) % 4][o + cy(L) * HX + cx(L)], q);
+        }
+      });
+      atomicAdd(&sacc[(z + 8) % 4][o], self);
+    }
+  };
 
   // Normals one plane ahead (kAhead): each plane takes one barrier, after which the normals
   // of plane z+2 go into the fourth ring slot while the collision of plane z reads planes
@@ -797,6 +868,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       });
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
+    if (kPush && z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
     if constexpr (kAhead) {
       if (z + 2 <= t.ze) normals(z + 2);
     } else {
@@ -809,7 +881,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     if (shell) {
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
-      if constexpr (EQ) {
+      if constexpr (kPush) {
+        // no flux; the shell's own next phi is the lagged copy of its nearest interior cell
+        push(z, pc, 0.f, 0.f, 0.f);
+        pnext[idx] = __ldg(pcur + clampi(x, 1, nx - 2) + clampi(y, 1, ny - 2) * nx +
+                           clampi(z, 1, nz - 2) * nxy);
+      } else if constexpr (EQ) {
         jout[idx] = make_float4(__int_as_float(pc), 0.f, 0.f, 0.f);
       } else {
         static_for<1, kQ>([&](auto LC) {
@@ -1027,8 +1104,10 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
     if constexpr (EQ) {
       // Equilibrium storage: the 18 populations are W_l (phi + c_l . J), J = 3 phi u + A n.
-      jout[idx] = make_float4(__int_as_float(pc), phi3 * ux + A * nc.x,
-                              phi3 * uy + A * nc.y, phi3 * uz + A * nc.z);
+      const float jx = phi3 * ux + A * nc.x, jy = phi3 * uy + A * nc.y;
+      const float jz = phi3 * uz + A * nc.z;
+      if constexpr (kPush) push(z, pc, jx, jy, jz);
+      else jout[idx] = make_float4(__int_as_float(pc), jx, jy, jz);
     } else {
       int sumq = 0;
       const GSplit sp = S::g_split(pc);
@@ -1049,6 +1128,11 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       a.macros[3 * T + o] = uy;
       a.macros[4 * T + o] = uz;
     }
+  }
+  if constexpr (kPush) {
+    // The last target planes of the run.
+    __syncthreads();
+    for (int q = max(t.ze - 2, t.zb - 1); q <= t.ze; ++q) flush(q);
   }
 }
 

@@ -75,6 +75,8 @@ struct StepArgs {
   int* rest_out;
   const int* p_prev;   // phi of the previous update, Q2.30
   int* p_cur;          // phi of this update, Q2.30
+  int* p_next;         // phi of the next update, accumulated by the collide kernel
+                       // (records not stored; zeroed before the launch), else nullptr
   float* macros;       // nullptr, or [5][cells_total]: phi, rho, ux, uy, uz
   void* j;             // kGEquil: 16-byte (P bits, Jx, Jy, Jz) per cell, at cell_off per case
   long long cells_total;
