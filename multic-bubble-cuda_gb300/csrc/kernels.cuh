@@ -769,19 +769,22 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   auto push = [&](int z, int P, float jx, float jy, float jz) {
     if constexpr (kPush) {
       const int o = (ty + 1) * HX + tx + 1;
+      int* s0 = sacc[(z + 8) % 4];
+      // targets of the cz = -1 and cz = +1 directions; across a z wall the cell itself
       const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
-      int self = wsplit_rest(P);
+      int* sm = blo ? s0 : sacc[(z + 7) % 4];
+      int* sp = bhi ? s0 : sacc[(z + 9) % 4];
+      const int om = blo ? 0 : 1, opl = bhi ? 0 : 1;  // 0: no shift in the plane
+      const int wfc = wsplit_face(P), wed = wsplit_edge_of_face(wfc);
+      atomicAdd(s0 + o, P - 6 * wfc - 12 * wed);  // the rest part
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
-        const int q = wsplit<L>(P) + qj<L>(jx, jy, jz);
-        const bool bounce = (cz(L) == -1) ? blo : ((cz(L) == 1) ? bhi : false);
-        if (bounce) {
-          self += q;
-        } else {
-          atomicAdd(&sacc[(z + cz(L) + 8) % 4][o + cy(L) * HX + cx(L)], q);
-        }
+        constexpr int D = cy(L) * HX + cx(L);
+        const int q = (L <= 6 ? wfc : wed) + qj<L>(jx, jy, jz);
+        if constexpr (cz(L) == 0) atomicAdd(s0 + o + D, q);
+        else if constexpr (cz(L) < 0) atomicAdd(sm + o + om * D, q);
+        else atomicAdd(sp + o + opl * D, q);
       });
-      atomicAdd(&sacc[(z + 8) % 4][o], self);
     }
   };
 
