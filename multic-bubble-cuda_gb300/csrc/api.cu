@@ -130,18 +130,21 @@ struct Solver {
   void* f[2] = {nullptr, nullptr};
   void* g[2] = {nullptr, nullptr};
   int* rest[2] = {nullptr, nullptr};
-  int* p[2] = {nullptr, nullptr};
+  // phi, Q2.30: two buffers alternate; the push mode rotates three (current, next,
+  // cleared for the one after)
+  int* p[3] = {nullptr, nullptr, nullptr};
   float* macros = nullptr;
   float* stage = nullptr;
   mcb::DiagPartial* partials = nullptr;
   mcb::DiagPartial* result = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph[6] = {};  // per (f parity, phi slot) at the start of the graph
   int graph_steps = 16;
   int ntiles = 0, zchunk = 16;
   int balanced = 1, phi_balanced = 0, planes = 0, grid_phi = 0, grid_collide = 0;
   int parity = 0, first = 1, latest_p = 1;
+  int pk = 0;  // current phi buffer; advances by one per update, modulo nphi()
   long long update = -1;
   std::vector<char> fields_set;
   std::vector<cudaEvent_t> prof_events;
@@ -151,6 +154,9 @@ struct Solver {
     MCB_CU(cudaSetDevice(device));
     return MCB_OK;
   }
+
+  int nphi() const { return push ? 3 : 2; }
+  int graph_key() const { return parity * 3 + pk; }
 
   void drop_graphs() {
     for (auto& ge : graph)
@@ -171,6 +177,8 @@ struct Solver {
       f[i] = g[i] = nullptr;
       rest[i] = p[i] = nullptr;
     }
+    cudaFree(p[2]);
+    p[2] = nullptr;
     cudaFree(macros);
     cudaFree(err);
     err = nullptr;
@@ -377,6 +385,7 @@ struct Solver {
     // (phi, J) records: with full g relaxation every collide kernel but the TMA one writes
     // the next phi itself; the TMA one keeps the records and the phi kernel.
     push = gmode == mcb::kGEquil && !padded;
+    if (push) MCB_CU(cudaMalloc(&p[2], cb));
     if (gmode == mcb::kGEquil && !push)
       MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * sizeof(float4)));
     MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
@@ -478,8 +487,9 @@ struct Solver {
     // A single case restarts from update 0 in buffer set 0.
     if (cases.size() == 1 || !stepped) {
       parity = 0;
+      pk = 0;
       first = 1;
-      latest_p = 1;
+      latest_p = nphi() - 1;
       update = -1;
       stepped = false;
     }
@@ -494,8 +504,10 @@ struct Solver {
     a.f1 = f[1];
     a.g0 = g[0];
     a.rest0 = rest[0];
-    a.p0 = p[0];
-    a.p1 = p[1];
+    // phi into the current buffer and the one diagnostics read; push: the next one cleared
+    a.p0 = p[pk];
+    a.p1 = p[(pk + nphi() - 1) % nphi()];
+    a.p_zero = push ? p[(pk + 1) % 3] : nullptr;
     a.macros = macros;
     a.cells_total = cells_total;
     a.gmode = gmode;
@@ -526,9 +538,10 @@ struct Solver {
     a.g_out = g[parity ^ 1];
     a.rest_in = rest[parity];
     a.rest_out = rest[parity ^ 1];
-    a.p_prev = p[parity ^ 1];
-    a.p_cur = p[parity];
-    a.p_next = push ? p[parity ^ 1] : nullptr;
+    a.p_prev = p[(pk + 1) % nphi()];
+    a.p_cur = p[pk];
+    a.p_next = push ? p[(pk + 1) % 3] : nullptr;
+    a.p_zero = push ? p[(pk + 2) % 3] : nullptr;
     a.macros = with_macros ? macros : nullptr;
     a.j = jbuf;
     a.cells_total = cells_total;
@@ -540,14 +553,19 @@ struct Solver {
   // takes phi from the init and runs only the collide kernel.
   bool skips_phi() const { return gmode == mcb::kGEquil && (push || first); }
 
-  // The phi stage of an update: the phi kernel, or (push) clearing the next phi.
+  // The phi stage of an update: the phi kernel, or nothing (push, first equilibrium update).
   int launch_phi_stage(const mcb::StepArgs& a) {
-    if (push)
-      MCB_CU(cudaMemsetAsync(p[parity ^ 1], 0, static_cast<size_t>(cells_total) * sizeof(int),
-                             stream));
-    else if (!skips_phi())
-      MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+    if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
     return MCB_OK;
+  }
+
+  // Moves to the next update's buffers.
+  void advance() {
+    latest_p = pk;
+    pk = (pk + 1) % nphi();
+    parity ^= 1;
+    first = 0;
+    ++update;
   }
 
   int launch_update(bool with_macros) {
@@ -555,19 +573,16 @@ struct Solver {
     MCB_TRY(launch_phi_stage(a));
     MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
                                stream));
-    latest_p = parity;
-    parity ^= 1;
-    first = 0;
-    ++update;
+    advance();
     return MCB_OK;
   }
 
-  // A graph of graph_steps updates (even) starting from buffer set `par`.
-  int ensure_graph(int par) {
-    if (graph[par]) return MCB_OK;
-    const int save_par = parity, save_first = first, save_latest = latest_p;
+  // A graph of graph_steps updates (even) starting from the current buffers.
+  int ensure_graph() {
+    const int key = graph_key();
+    if (graph[key]) return MCB_OK;
+    const int save_par = parity, save_pk = pk, save_first = first, save_latest = latest_p;
     const long long save_update = update;
-    parity = par;
     first = 0;
     cudaGraph_t gr = nullptr;
     MCB_CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -575,6 +590,7 @@ struct Solver {
     for (int i = 0; i < graph_steps && rc == MCB_OK; ++i) rc = launch_update(false);
     const cudaError_t ec = cudaStreamEndCapture(stream, &gr);
     parity = save_par;
+    pk = save_pk;
     first = save_first;
     latest_p = save_latest;
     update = save_update;
@@ -584,7 +600,7 @@ struct Solver {
     }
     if (ec != cudaSuccess)
       return fail(MCB_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
-    const cudaError_t ei = cudaGraphInstantiate(&graph[par], gr, 0);
+    const cudaError_t ei = cudaGraphInstantiate(&graph[key], gr, 0);
     cudaGraphDestroy(gr);
     if (ei != cudaSuccess)
       return fail(MCB_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
@@ -605,10 +621,11 @@ struct Solver {
         MCB_TRY(launch_update(remaining == 1));
         --remaining;
       } else {
-        MCB_TRY(ensure_graph(parity));
-        MCB_CU(cudaGraphLaunch(graph[parity], stream));
-        // The graph leaves the buffer parity unchanged (even length).
-        latest_p = parity ^ 1;
+        MCB_TRY(ensure_graph());
+        MCB_CU(cudaGraphLaunch(graph[graph_key()], stream));
+        // The graph leaves the f parity unchanged (even length) and moves the phi slot on.
+        pk = (pk + graph_steps) % nphi();
+        latest_p = (pk + nphi() - 1) % nphi();
         update += graph_steps;
         remaining -= graph_steps;
       }
@@ -640,10 +657,7 @@ struct Solver {
       MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
                                stream));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 2], stream));
-      latest_p = parity;
-      parity ^= 1;
-      first = 0;
-      ++update;
+      advance();
     }
     MCB_CU(cudaEventRecord(ev1, stream));
     stepped = true;
@@ -668,7 +682,7 @@ struct Solver {
   // ---- checkpoint: header + raw device buffers ----
   struct CkptHeader {
     char magic[8];
-    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad, qf, ratio, pad2;
+    int abi, nx, ny, nz, bc, storage, gmode, parity, first, latest_p, pad, qf, ratio, pk;
     long long update;
     float tau, tau_g, sigma, sharp_c, gravity, phi_mean;
   };
@@ -684,8 +698,7 @@ struct Solver {
       v.push_back({g[parity], n * 18 * pop_bytes(storage)});
       v.push_back({rest[parity], n * sizeof(int)});
     }
-    v.push_back({p[0], n * sizeof(int)});
-    v.push_back({p[1], n * sizeof(int)});
+    for (int i = 0; i < nphi(); ++i) v.push_back({p[i], n * sizeof(int)});
     v.push_back({macros, n * 5 * sizeof(float)});
     return v;
   }
@@ -709,6 +722,7 @@ struct Solver {
     hd.parity = parity;
     hd.first = first;
     hd.latest_p = latest_p;
+    hd.pk = pk;
     hd.pad = padded ? cases[0].fgx : 0;  // f layout
     hd.qf = qf;
     hd.ratio = ratio;
@@ -781,6 +795,7 @@ struct Solver {
     MCB_CU(cudaMemcpy(f[parity ^ 1], f[parity], f_bytes(), cudaMemcpyDeviceToDevice));
     first = hd.first;
     latest_p = hd.latest_p;
+    pk = push ? hd.pk : parity;
     update = hd.update;
     d.phi_mean = hd.phi_mean;
     MCB_CU(cudaMemcpy(d_cases, &d, sizeof d, cudaMemcpyHostToDevice));
@@ -1130,12 +1145,13 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     cudaFree(ms);
   };
   if (cudaMalloc(&fs, fb) != cudaSuccess || (gb && cudaMalloc(&gs, gb) != cudaSuccess) ||
-      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 8) != cudaSuccess ||
+      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 12) != cudaSuccess ||
       cudaMalloc(&ms, n * 20) != cudaSuccess) {
     free_all();
     return fail(MCB_ERR_ALLOC, "autotune: no room for a state copy");
   }
   const int save_first = s.first, save_latest = s.latest_p, save_variant = s.variant;
+  const int save_pk = s.pk;
   const int save_zreq = s.zchunk_req;
   const long long save_update = s.update;
   auto snapshot = [&](bool restore) -> int {
@@ -1147,15 +1163,15 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
       if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
       if (e == cudaSuccess && gb) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
       if (e == cudaSuccess && !eq) e = cp(rs, s.rest[par], n * 4);
-      if (e == cudaSuccess) e = cp(ps, s.p[0], n * 4);
-      if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + n * 4, s.p[1], n * 4);
+      for (int i = 0; i < s.nphi(); ++i)
+        if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + i * n * 4, s.p[i], n * 4);
       if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
     } else {
       if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
       if (e == cudaSuccess && gb) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
       if (e == cudaSuccess && !eq) e = cp(s.rest[par], rs, n * 4);
-      if (e == cudaSuccess) e = cp(s.p[0], ps, n * 4);
-      if (e == cudaSuccess) e = cp(s.p[1], static_cast<char*>(ps) + n * 4, n * 4);
+      for (int i = 0; i < s.nphi(); ++i)
+        if (e == cudaSuccess) e = cp(s.p[i], static_cast<char*>(ps) + i * n * 4, n * 4);
       if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);
       // Reference-mode shells keep f = W_l in both buffers; the other buffer's interior
       // is rewritten by the next update.
@@ -1164,6 +1180,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) return fail(MCB_ERR_CUDA, "autotune copy: %s", cudaGetErrorString(e));
     s.parity = par;
+    s.pk = save_pk;
     s.first = save_first;
     s.latest_p = save_latest;
     s.update = save_update;

@@ -657,6 +657,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   constexpr bool kPush = EQ && !kTma;
   __shared__ int sacc[kPush ? 4 : 1][kPush ? HP : 1];
   int* __restrict__ pnext = kPush ? a.p_next + t.cell_off : nullptr;
+  int* __restrict__ pzero = kPush ? a.p_zero + t.cell_off : nullptr;
   // Global in-plane offsets of this thread's two accumulator positions (-1: none).
   int aoff[2] = {-1, -1};
   if constexpr (kPush) {
@@ -881,6 +882,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     if (!active) continue;
 
     const int pc = __ldg(pcur + idx);
+    if constexpr (kPush) pzero[idx] = 0;  // the next update accumulates into it
     if (shell) {
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
@@ -1219,6 +1221,7 @@ __global__ void k_init(const InitArgs a) {
   const int P = (eq && shell) ? 0 : __float2int_rn(phi_self * kQ30);
   a.p0[co + idx] = P;
   a.p1[co + idx] = P;
+  if (a.p_zero) a.p_zero[co + idx] = 0;
   const float ux_s = a.ux ? a.ux[idx] : 0.f;
   const float uy_s = a.uy ? a.uy[idx] : 0.f;
   const float uz_s = a.uz ? a.uz[idx] : 0.f;

@@ -76,7 +76,9 @@ struct StepArgs {
   const int* p_prev;   // phi of the previous update, Q2.30
   int* p_cur;          // phi of this update, Q2.30
   int* p_next;         // phi of the next update, accumulated by the collide kernel
-                       // (records not stored; zeroed before the launch), else nullptr
+                       // (records not stored; zero before the launch), else nullptr
+  int* p_zero;         // with p_next: the phi buffer of the update after the next one,
+                       // cleared by the collide kernel (three buffers rotate)
   float* macros;       // nullptr, or [5][cells_total]: phi, rho, ux, uy, uz
   void* j;             // kGEquil: 16-byte (P bits, Jx, Jy, Jz) per cell, at cell_off per case
   long long cells_total;
@@ -96,6 +98,7 @@ struct InitArgs {
   int* rest0;
   int* p0;
   int* p1;
+  int* p_zero;        // nullptr, or a phi buffer to clear (the next phi of the push mode)
   float* macros;
   long long cells_total;
   int gmode;
