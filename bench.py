@@ -5,8 +5,8 @@ Workload: the rising perturbed bubble:
   - gravity 1e-5, R 16 at z 48, spherical-harmonic modes l = 2..6;
   - tau 0.7, sigma 0.05, W 4;
   - FP32 storage, seeded synthetic initial field.
-A step is one lattice update of the whole lattice. Inputs exceed L2: the f populations and
-(phi, J) records one update reads hold 386 MB.
+A step is one lattice update of the whole lattice. Inputs exceed L2: the f populations one
+update reads and writes hold 638 MB.
 
   value     MLUPS with the state resident in HBM: cells * K / device time of K updates,
             CUDA events on the solver's stream, max over ranks. An event after every
@@ -41,38 +41,52 @@ sys.path.insert(0, str(REPO / "multic-bubble-cuda_gb300"))
 
 METRIC = "MLUPS and % HBM roofline; FP16-store vs FP32 at fixed Laplace-law error"
 SCENARIO, SEED = 2, 1
-# Algorithmic bytes per lattice update and kernel, (phi kernel, collide kernel), each array
-# read or written once per cell.
-#   equilibrium g storage (tau_g = 1, the default): k_phi_eq reads the 16-byte (P, J) record
-#     and writes P (4 B). k_collide reads and writes f (19 populations), reads P and writes
-#     the record. 16-bit storage also reads the previous P, the base of the deviation form.
-#   stored g populations (tau_g != 1): k_phi reads g (18 populations) and the rest
-#     population; k_collide reads and writes f and writes g.
-BYTES = {
-    "equilibrium": {"f32": (20, 172), "f16": (20, 100), "bf16": (20, 100)},
-    "populations": {"f32": (76, 228), "f16": (38, 114), "bf16": (38, 114)},
-}
+TMA_VARIANT = 4
 
 
-def g_storage(cfg) -> str:
+def g_storage(cfg, variant: int = -1) -> str:
+    """How the phase field crosses an update.
+      push         g at equilibrium (tau_g = 1, the default): the collide kernel adds each
+                   cell's integer populations into the next phi; no phi kernel
+      records      the same g, with a 16-byte (P, J) record per cell and the phi kernel
+                   (the TMA-staged collide)
+      populations  stored g populations (tau_g != 1) and the phi kernel"""
     import mcb
 
-    return ("equilibrium" if cfg.tau_g == 1.0 and cfg.g_mode != mcb.G_POPULATIONS
-            else "populations")
+    if cfg.tau_g != 1.0 or cfg.g_mode == mcb.G_POPULATIONS:
+        return "populations"
+    return "records" if variant == TMA_VARIANT else "push"
 
 
-def bytes_per_lu(cfg, storage: str) -> tuple[int, int, int]:
-    """(phi kernel, collide kernel, whole update) algorithmic bytes per lattice update."""
-    ph, col = BYTES[g_storage(cfg)][storage]
+def bytes_per_lu(cfg, storage: str, variant: int = -1) -> tuple[int, int, int]:
+    """(phi kernel, collide kernel, whole update) algorithmic bytes per lattice update:
+    each array a kernel reads or writes, once per cell.
+      push         collide: f in and out (Q populations), phi in, the next phi (integer
+                   atomics into L2, counted once), the phi buffer after next cleared (4 B)
+      records      phi kernel: the record in, phi out; collide: f in and out, phi in, record out
+      populations  phi kernel: 18 g and the rest in, phi out, and the previous phi in with
+                   16-bit storage (the base of its deviation form); collide: f in and out,
+                   phi in, 18 g and the rest out"""
+    pb = 4 if storage == "f32" else 2
+    q = 27 if cfg.velocity_set == 27 else 19
+    f = 2 * q * pb
+    gs = g_storage(cfg, variant)
+    if gs == "push":
+        ph, col = 0, f + 4 + 4 + 4
+    elif gs == "records":
+        ph, col = 16 + 4, f + 4 + 16
+    else:
+        ph = 18 * pb + 4 + 4 + (4 if storage != "f32" else 0)
+        col = f + 4 + 18 * pb + 4
     return ph, col, ph + col
 
 
-def footprint_bytes(cells: int, storage: str, gs: str) -> int:
-    """Device bytes of one solver handle: f ping-pong, g state, phi ping-pong, macros,
+def footprint_bytes(cells: int, storage: str, gs: str, q: int = 19) -> int:
+    """Device bytes of one solver handle: f ping-pong, g state, phi buffers, macros,
     host-upload staging."""
     pb = 4 if storage == "f32" else 2
-    g = cells * 16 if gs == "equilibrium" else 2 * cells * (18 * pb + 4)
-    return 2 * cells * 19 * pb + g + 2 * cells * 4 + cells * 5 * 4 + cells * 4 * 4
+    g = {"push": cells * 4, "records": cells * 16}.get(gs, 2 * cells * (18 * pb + 4))
+    return 2 * cells * q * pb + g + 2 * cells * 4 + cells * 5 * 4 + cells * 4 * 4
 
 
 def dist_env():
@@ -304,10 +318,9 @@ def d3q27_run(device, steps, storage="f32"):
         s.set_fields(phi, ux, uy, uz)
         s.step(20)
         total, t_phi, t_col = s.step_profiled(steps)
-    pb = 4 if storage == "f32" else 2
-    col_bytes = 2 * 27 * pb + 4 + 16 + (4 if storage != "f32" else 0)
+    col_bytes = bytes_per_lu(cfg, storage)[1]
     return {"storage": storage, "steps": steps, "mlups": cells * steps / (total * 1e-3) / 1e6,
-            "kernel_ms": {"k_phi": t_phi / steps, "k_collide": t_col / steps},
+            "kernel_ms": {"phi_stage": t_phi / steps, "k_collide": t_col / steps},
             "collide_bytes_per_lu": col_bytes,
             "collide_gbs_algorithmic": col_bytes * cells / (t_col * 1e-3 / steps) / 1e9}
 
@@ -332,7 +345,7 @@ def swarm_run(device, steps):
             "hbm_gbs_algorithmic": bytes_per_lu(cfg, "f16")[2] * cells / per_update / 1e9,
             "mass_drift_q30": int(d["mass_q30"] - m0),
             "footprint_gb": footprint_bytes(cells, "f16", gs) / 1e9,
-            "kernel_ms": {"k_phi": t_phi / steps, "k_collide": t_col / steps}}
+            "kernel_ms": {"phi_stage": t_phi / steps, "k_collide": t_col / steps}}
 
 
 def cpu_baseline(seconds=10.0, threads=None):
@@ -356,7 +369,7 @@ def cpu_baseline(seconds=10.0, threads=None):
                       f" {n} updates in {dt:.1f} s"}
 
 
-def traffic_per_launch(cells, storage="f32", gs="equilibrium"):
+def traffic_per_launch(cells, storage="f32", gs="push"):
     """DRAM bytes per collide launch, from the committed ncu capture of this workload
     (profiles/traffic.json, bytes per cell), times the cells of one launch."""
     p = REPO / "profiles" / "traffic.json"
@@ -415,7 +428,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched-cases and 512^3 swarm legs")
     ap.add_argument("--g-populations", action="store_true",
-                    help="store the 19 g populations instead of the (phi, J) records")
+                    help="store the 18 moving g populations (the phi kernel reads them)")
     ap.add_argument("--variant", type=int, default=-1,
                     help="tile variant of the device leg (-1 default; 4 the TMA-staged collide)")
     ap.add_argument("--zchunk", type=int, default=0,
@@ -454,8 +467,8 @@ def main():
     hbm, peak_kind = peaks()
     col_avg_s = col_ms * 1e-3 / args.steps
     st = args.storage
-    gs = g_storage(cfg)
-    _, col_b, upd_b = bytes_per_lu(cfg, st)
+    gs = g_storage(cfg, VARIANT)
+    _, col_b, upd_b = bytes_per_lu(cfg, st, VARIANT)
     achieved = col_b * cells / col_avg_s / 1e9
     update_achieved = upd_b * cells / (total_ms * 1e-3 / args.steps) / 1e9
     result = {
@@ -466,7 +479,8 @@ def main():
         "config": {"workload": f"rising perturbed bubble {cfg.nx}x{cfg.ny}x{cfg.nz}, walls z, "
                                "gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 "
                                "storage",
-                   "cells": cells, "l2": "inputs larger than L2 (f + records 386 MB per update)",
+                   "cells": cells,
+                   "l2": "inputs larger than L2 (f in and out: 638 MB per update, FP32)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
         "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
@@ -475,8 +489,9 @@ def main():
                      "traffic": traffic_per_launch(cells, st, gs),
                      "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
                      "update_bytes_per_lu": upd_b,
-                     "kernel_ms": {"k_phi": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
-        "gpu_launches": 2 * args.steps,
+                     "kernel_ms": {"phi_stage": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
+        # push: one collide launch per update; else the phi kernel and the collide kernel
+        "gpu_launches": (1 if gs == "push" else 2) * args.steps,
         "clocks": clk.summary(),
         "mass_q30_finite": bool(diag["finite"]),
     }
@@ -486,9 +501,9 @@ def main():
         _, t16, p16, c16, d16 = device_run("f16", local, args.steps, args.warmup, None)
         v16 = cells * args.steps / (t16 * 1e-3) / 1e6
         result["fp16"] = {"value": v16, "unit": "MLUPS", "ratio_vs_f32": v16 / (value / ws),
-                          "frac_update": bytes_per_lu(cfg, "f16")[2] * cells
+                          "frac_update": bytes_per_lu(cfg, "f16", VARIANT)[2] * cells
                           / (t16 * 1e-3 / args.steps) / 1e9 / hbm,
-                          "kernel_ms": {"k_phi": p16 / args.steps, "k_collide": c16 / args.steps}}
+                          "kernel_ms": {"phi_stage": p16 / args.steps, "k_collide": c16 / args.steps}}
         result["e2e"] = e2e_run(local, args.steps)
         if not args.no_extras:
             result["batch"] = batch_run(local, min(args.steps, 200))

@@ -88,10 +88,12 @@ typedef struct mcb_config {
     int   use_graph;    /* 1 = replay updates from a CUDA graph, 0 = plain launches */
     int   g_mode;       /* how g crosses between updates:
                            MCB_G_AUTO: with tau_g = 1 every post-collision g population is
-                             the equilibrium W_l (phi + c_l.J) of its cell, so only
-                             J = 3 phi u + sharp_c phi (1 - phi) n is stored and the next
-                             update rebuilds the populations; with tau_g != 1 all 19 are
-                             stored;
+                             the equilibrium W_l (phi + c_l.J) of its cell,
+                             J = 3 phi u + sharp_c phi (1 - phi) n: the collide kernel adds
+                             the 19 populations, as exact Q2.30 integers, straight into the
+                             next update's phi and no g is stored (the TMA variant stores
+                             (phi, J) per cell and rebuilds them); with tau_g != 1 all 19
+                             are stored;
                            MCB_G_POPULATIONS: always store the 19 populations. */
     int   velocity_set; /* velocity set of f: 19 (D3Q19, the reference's build) or 27
                            (D3Q27 with the tables of src/var.cu:33-35,47-52; the
@@ -200,8 +202,9 @@ int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
 /* Checkpoint and restart. No counterpart in the reference, which saves only phi
  * (src/main.cu:184-189) and so cannot resume. mcb_checkpoint_save writes everything the
  * next update reads:
- *   - the populations (or, with equilibrium g storage, the per-cell (phi, J) records);
- *   - both phi buffers;
+ *   - the f populations, and the g populations (or the (phi, J) records of the TMA
+ *     variant) where g is stored;
+ *   - every phi buffer (two, or three in the default equilibrium g mode);
  *   - the fields of the latest update;
  *   - the update counter, the buffer parity and the buoyancy reference;
  * together with the configuration. mcb_checkpoint_load restores them into a handle created
@@ -220,7 +223,9 @@ int  mcb_last_step_ms(mcb_handle* h, float* ms);
 
 /* Like mcb_step, but with plain launches and a CUDA event after every kernel, for
  * measurement. On return: total_ms is the device time from the first launch to the last;
- * phi_ms and collide_ms are the summed durations of the two kernels of every update. */
+ * phi_ms is the summed time from the end of one update to its collide launch (the phi
+ * kernel where there is one, else the gap between launches); collide_ms is the summed
+ * duration of the collide kernels. */
 int  mcb_step_profiled(mcb_handle* h, int nsteps, float* total_ms, float* phi_ms,
                        float* collide_ms);
 
