@@ -369,31 +369,37 @@ __global__ void __launch_bounds__(BX * BY, phi_warps_per_sm<S>() * 32 / (BX * BY
 //   g*_l = W_l (phi + c_l . J),  J = 3 phi u + SHARP_C phi (1 - phi) n
 // (src/lbm.cu:319-326). Its Q2.30 value is stored implicitly as two parts:
 //   - the exact integer weight split w_l(P) of the cell's phi, which sums to P over l;
-//   - q_J(l) = rn(W_l c_l.J 2^30), whose opposite directions are exact negatives.
+//   - q_J(l) = m_l c_l.J', with J' = rn(J 2^30 / 36) per component (integers) and
+//     m_l = 2 on the faces (W = 1/18), 1 on the edges (W = 1/36): W_l c_l.J 2^30 to within
+//     one unit per component. Opposite directions are exact negatives.
 // The 18 moving parts of a cell therefore add up to P - w_0(P): the rest population is
 // exactly w_0(P), and the lattice sum of phi is invariant. Each cell keeps one 16-byte
-// record of the update: (P as int bits, Jx, Jy, Jz).
+// record of the update: (P, J'x, J'y, J'z) as int bits.
+
+// J' of a cell.
+struct JQ {
+  int x, y, z;
+};
+__device__ __forceinline__ JQ jq_of(float jx, float jy, float jz) {
+  constexpr float k = 1073741824.0f / 36.0f;
+  return JQ{__float2int_rn(jx * k), __float2int_rn(jy * k), __float2int_rn(jz * k)};
+}
 
 // q_J for direction L (its opposite is the exact negative).
 template <int L>
-__device__ __forceinline__ int qj(float jx, float jy, float jz) {
-  constexpr float kWq = static_cast<float>(wd(L) * 1073741824.0);
-  // c_l . J with at most two nonzero terms, added without contraction.
-  const float a = cx(L) != 0 ? (cx(L) > 0 ? jx : -jx) : (cy(L) > 0 ? jy : -jy);
-  const float b = cx(L) != 0 ? (cy(L) != 0 ? (cy(L) > 0 ? jy : -jy)
-                                           : (cz(L) != 0 ? (cz(L) > 0 ? jz : -jz) : 0.f))
-                             : (cy(L) != 0 ? (cz(L) != 0 ? (cz(L) > 0 ? jz : -jz) : 0.f)
-                                           : 0.f);
-  const bool two = (cx(L) != 0) + (cy(L) != 0) + (cz(L) != 0) == 2;
-  const float cj = cy(L) == 0 && cx(L) == 0 ? (cz(L) > 0 ? jz : -jz)
-                 : (two ? __fadd_rn(a, b) : a);
-  return __float2int_rn(__fmul_rn(cj, kWq));
+__device__ __forceinline__ int qj(const JQ& j) {
+  int cj = 0;
+  if constexpr (cx(L) != 0) cj += cx(L) > 0 ? j.x : -j.x;
+  if constexpr (cy(L) != 0) cj += cy(L) > 0 ? j.y : -j.y;
+  if constexpr (cz(L) != 0) cj += cz(L) > 0 ? j.z : -j.z;
+  return L <= 6 ? 2 * cj : cj;
 }
 
-// Q2.30 population L of a cell record (P, Jx, Jy, Jz).
+// Q2.30 population L of a cell record (P, J'x, J'y, J'z).
 template <int L>
 __device__ __forceinline__ int q_rec(float4 r) {
-  return wsplit<L>(__float_as_int(r.x)) + qj<L>(r.y, r.z, r.w);
+  return wsplit<L>(__float_as_int(r.x)) +
+         qj<L>(JQ{__float_as_int(r.y), __float_as_int(r.z), __float_as_int(r.w)});
 }
 
 template <class S, int BX, int BY>
@@ -648,7 +654,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       if (tid + k * NT < PP) d[tid + k * NT] = __int2float_rn(pre[k]) * kInvQ30;
   };
   // kPush: the collide kernel writes the next update's phi itself. Each cell s pushes its
-  // 19 exact Q2.30 populations q_l = w_l(P_s) + rn(W_l c_l.J_s 2^30) to their consumers
+  // 19 exact Q2.30 populations q_l = w_l(P_s) + m_l c_l.J'_s to their consumers
   // s + c_l (the same integers the record rebuild pulls): inside the tile through a
   // 4-plane shared ring of integer sums (tile + halo 1), flushed to global memory with
   // integer atomic adds once a target plane is complete. Integer sums do not depend on the
@@ -764,10 +770,10 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
   }
 
-  // Pushes the populations of source cell (x, y, z), phi P and flux (jx, jy, jz), into the
+  // Pushes the populations of source cell (x, y, z), phi P and integer flux J', into the
   // shared ring: q_l to target plane z + cz(l), the rest part and populations bounced at a
   // z wall to the cell itself.
-  auto push = [&](int z, int P, float jx, float jy, float jz) {
+  auto push = [&](int z, int P, const JQ& jq) {
     if constexpr (kPush) {
       const int o = (ty + 1) * HX + tx + 1;
       int* s0 = sacc[(z + 8) % 4];
@@ -781,7 +787,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
         constexpr int D = cy(L) * HX + cx(L);
-        const int q = (L <= 6 ? wfc : wed) + qj<L>(jx, jy, jz);
+        const int q = (L <= 6 ? wfc : wed) + qj<L>(jq);
         if constexpr (cz(L) == 0) atomicAdd(s0 + o + D, q);
         else if constexpr (cz(L) < 0) atomicAdd(sm + o + om * D, q);
         else atomicAdd(sp + o + opl * D, q);
@@ -888,11 +894,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       // (fgBoundary, src/lbm.cu:391-400); its f stays at W_l (rho_b = 1) from the init.
       if constexpr (kPush) {
         // no flux; the shell's own next phi is the lagged copy of its nearest interior cell
-        push(z, pc, 0.f, 0.f, 0.f);
+        push(z, pc, JQ{0, 0, 0});
         pnext[idx] = __ldg(pcur + clampi(x, 1, nx - 2) + clampi(y, 1, ny - 2) * nx +
                            clampi(z, 1, nz - 2) * nxy);
       } else if constexpr (EQ) {
-        jout[idx] = make_float4(__int_as_float(pc), 0.f, 0.f, 0.f);
+        jout[idx] = make_float4(__int_as_float(pc), __int_as_float(0), __int_as_float(0),
+                                __int_as_float(0));
       } else {
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
@@ -1109,10 +1116,11 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
     if constexpr (EQ) {
       // Equilibrium storage: the 18 populations are W_l (phi + c_l . J), J = 3 phi u + A n.
-      const float jx = phi3 * ux + A * nc.x, jy = phi3 * uy + A * nc.y;
-      const float jz = phi3 * uz + A * nc.z;
-      if constexpr (kPush) push(z, pc, jx, jy, jz);
-      else jout[idx] = make_float4(__int_as_float(pc), jx, jy, jz);
+      const JQ jq = jq_of(phi3 * ux + A * nc.x, phi3 * uy + A * nc.y, phi3 * uz + A * nc.z);
+      if constexpr (kPush) push(z, pc, jq);
+      else
+        jout[idx] = make_float4(__int_as_float(pc), __int_as_float(jq.x), __int_as_float(jq.y),
+                                __int_as_float(jq.z));
     } else {
       int sumq = 0;
       const GSplit sp = S::g_split(pc);
