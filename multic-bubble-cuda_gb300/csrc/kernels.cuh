@@ -703,6 +703,20 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
   };
 
+  // Phi-plane offset of normals point i (the same on every plane), -1 where (reference
+  // mode) the point is on or beyond the shell in x or y and its normal is 0. The 32-bit
+  // offset kernels read them from a table filled here (the rings fill after the barrier
+  // that follows); the 64-bit ones compute them per plane (measured 3 % faster there).
+  constexpr bool kCenTab = !kWide;
+  auto center = [&](int i) {
+    const int hx = i % HX, hy = i / HX;
+    const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
+    const bool zero = ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1);
+    return zero ? -1 : (hy + 1) * PX + hx + 1;
+  };
+  __shared__ int scen[kCenTab ? HP : 1];
+  if constexpr (kCenTab)
+    for (int i = tid; i < HP; i += NT) scen[i] = center(i);
   // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72).
   auto normals = [&](int zp) {
     const float* pm = sphi[(zp + 4) % 5];
@@ -711,12 +725,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     float(*dst)[HP] = snrm[(zp + 4) % 4];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
     for (int i = tid; i < HP; i += NT) {
-      const int hx = i % HX, hy = i / HX;
-      const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
+      const int c = kCenTab ? scen[i] : center(i);
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-      const bool zero = zshell || (ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1));
-      if (!zero) {
-        const int c = (hy + 1) * PX + hx + 1;
+      if (c >= 0 && !zshell) {
         float gxs = 0.f, gys = 0.f, gzs = 0.f;
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
@@ -776,22 +787,31 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   auto push = [&](int z, int P, const JQ& jq) {
     if constexpr (kPush) {
       const int o = (ty + 1) * HX + tx + 1;
-      int* s0 = sacc[(z + 8) % 4];
-      // targets of the cz = -1 and cz = +1 directions; across a z wall the cell itself
-      const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
-      int* sm = blo ? s0 : sacc[(z + 7) % 4];
-      int* sp = bhi ? s0 : sacc[(z + 9) % 4];
-      const int om = blo ? 0 : 1, opl = bhi ? 0 : 1;  // 0: no shift in the plane
+      int* s0 = &sacc[(z + 8) & 3][o];
+      int* sm = &sacc[(z + 7) & 3][o];
+      int* sp = &sacc[(z + 9) & 3][o];
       const int wfc = wsplit_face(P), wed = wsplit_edge_of_face(wfc);
-      atomicAdd(s0 + o, P - 6 * wfc - 12 * wed);  // the rest part
-      static_for<1, kQ>([&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        constexpr int D = cy(L) * HX + cx(L);
-        const int q = (L <= 6 ? wfc : wed) + qj<L>(jq);
-        if constexpr (cz(L) == 0) atomicAdd(s0 + o + D, q);
-        else if constexpr (cz(L) < 0) atomicAdd(sm + o + om * D, q);
-        else atomicAdd(sp + o + opl * D, q);
-      });
+      atomicAdd(s0, P - 6 * wfc - 12 * wed);  // the rest part
+      if (walls && (z == 0 || z == nz - 1)) {
+        // A wall plane: what leaves through the wall returns to the cell itself.
+        const bool blo = z == 0, bhi = z == nz - 1;
+        static_for<1, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          constexpr int D = cy(L) * HX + cx(L);
+          const int q = (L <= 6 ? wfc : wed) + qj<L>(jq);
+          const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
+          int* tgt = cz(L) < 0 ? sm + D : (cz(L) > 0 ? sp + D : s0 + D);
+          atomicAdd(bounce ? s0 : tgt, q);
+        });
+      } else {
+        // Every other plane: fixed shared offsets (immediates of the atomics).
+        static_for<1, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          constexpr int D = cy(L) * HX + cx(L);
+          int* b = cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0);
+          atomicAdd(b + D, (L <= 6 ? wfc : wed) + qj<L>(jq));
+        });
+      }
     }
   };
 
