@@ -881,21 +881,31 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
                             t.yt, z + 2, nz, t.bc, t.fgx);
     } else if (work) {
       fr[0] = S::fload(fin + idx);
-      static_for<1, QF>([&](auto LC) {
+      // 32-bit: one signed offset; 64-bit: the base pointer first (cheaper there).
+      auto pull = [&](auto LC) {
         constexpr int L = decltype(LC)::value;
-        constexpr int O = opp(L);
-        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
-        if (bounce) {
-          // 32-bit: one signed offset; 64-bit: the base pointer first (cheaper there).
-          if constexpr (kWide) fr[L] = S::fload(fin + O * n + idx);
-          else fr[L] = S::fload(fin + (O * n + idx));
-        } else {
-          const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
-                        src_of<cx(L)>(xm, x, xp);
-          if constexpr (kWide) fr[L] = S::fload(fin + L * n + s);
-          else fr[L] = S::fload(fin + (L * n + s));
-        }
-      });
+        const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                      src_of<cx(L)>(xm, x, xp);
+        if constexpr (kWide) fr[L] = S::fload(fin + L * n + s);
+        else fr[L] = S::fload(fin + (L * n + s));
+      };
+      if (blo || bhi) {
+        // A wall plane: what left through the wall returns as the cell's own opposite
+        // population.
+        static_for<1, QF>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          constexpr int O = opp(L);
+          const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+          if (bounce) {
+            if constexpr (kWide) fr[L] = S::fload(fin + O * n + idx);
+            else fr[L] = S::fload(fin + (O * n + idx));
+          } else {
+            pull(LC);
+          }
+        });
+      } else {
+        static_for<1, QF>(pull);
+      }
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
     if (kPush && z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
