@@ -116,6 +116,7 @@ struct Solver {
   std::vector<mcb_config> cfg;
   std::vector<mcb::CaseDesc> cases;
   long long cells_total = 0, max_cells = 0;
+  long long f_cells_total = 0, max_f_cells = 0;  // cells of the f layout (x rounded up to 32)
   bool bgk = false;
   int gmode = mcb::kGPop;
   int qf = 19;             // velocity set of f
@@ -317,7 +318,6 @@ struct Solver {
       d.bc = c.bc;
       d.ncell = static_cast<long long>(c.nx) * c.ny * c.nz;
       d.cell_off = off;
-      d.f_off = off * qf;
       d.g_off = off * 18;
       d.omega = 1.0f / c.tau;
       d.omega_g = 1.0f / c.tau_g;
@@ -344,11 +344,26 @@ struct Solver {
     padded = n == 1 && qf == 19 && !ratio && gmode == mcb::kGEquil &&
              cs[0].nx % (gxe / 2) == 0 &&
              cs[0].variant == mcb::kTmaVariant && encode_fn() != nullptr;
-    // 32-bit f offsets need qf * cells < 2^31 in every case; larger cases run the 32x8
-    // tile with 64-bit offsets. MCB_WIDE_OFFSETS=1 forces those on any size (the tests
-    // compare the two).
+    // 32-bit f offsets need qf * cells < 2^31 in every case (cells of the blocked layout,
+    // x rounded up to 32); larger cases run the 32x8 tile with 64-bit offsets.
+    // MCB_WIDE_OFFSETS=1 forces those on any size (the tests compare the two).
+    long long max_blocked = 0;
+    for (auto& d : cases)
+      max_blocked = std::max(max_blocked, ((d.nx + 31) / 32) * 32LL * d.ny * d.nz);
     const char* force_wide = std::getenv("MCB_WIDE_OFFSETS");
-    wide = max_cells * qf >= (1LL << 31) || (force_wide && force_wide[0] == '1');
+    wide = max_blocked * qf >= (1LL << 31) || (force_wide && force_wide[0] == '1');
+    // f layout: blocked with equilibrium g and 32-bit offsets (x rounded up to whole 32-cell
+    // blocks); plain otherwise (the 64-bit kernels and the stored-g ones measured slower
+    // blocked: they spill the extra per-thread offsets). The padded TMA layout is set below.
+    const bool blocked = gmode == mcb::kGEquil && !wide;
+    f_cells_total = max_f_cells = 0;
+    for (auto& d : cases) {
+      d.fxb = blocked ? (d.nx + 31) / 32 : 0;
+      const long long fc = blocked ? static_cast<long long>(d.fxb) * 32 * d.ny * d.nz : d.ncell;
+      d.f_off = f_cells_total * qf;
+      f_cells_total += fc;
+      max_f_cells = std::max(max_f_cells, fc);
+    }
     if (wide) padded = false;
     if (padded) variant = mcb::kTmaVariant;
     else if (variant == mcb::kTmaVariant || qf == 27 || ratio || wide) variant = 0;
@@ -359,6 +374,7 @@ struct Solver {
         d.fpy = d.ny + 2;
         d.fn = static_cast<long long>(d.fpx) * d.fpy * d.nz;
         d.f_off = 0;
+        d.fxb = 0;
       } else {
         d.fgx = 0;
         d.fpx = d.nx;
@@ -403,7 +419,7 @@ struct Solver {
   }
 
   size_t f_bytes() const {
-    const long long per = padded ? cases[0].fn : cells_total;
+    const long long per = padded ? cases[0].fn : f_cells_total;
     return static_cast<size_t>(per) * qf * pop_bytes(storage);
   }
 

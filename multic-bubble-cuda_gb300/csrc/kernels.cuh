@@ -213,7 +213,7 @@ __device__ __forceinline__ int find_case(const CaseDesc* cs, int n, int key) {
 
 struct Tile {
   int nx, ny, nz, bc, zb, ze, xt, yt, ci;
-  int fgx, fpx, fpy;
+  int fgx, fpx, fpy, fxb;
   long long ncell, cell_off, f_off, g_off, fn;
 };
 
@@ -259,6 +259,7 @@ __device__ __forceinline__ Tile segment_tile(const StepArgs& a, int p, int p1) {
   t.fgx = __ldg(&cd->fgx);
   t.fpx = __ldg(&cd->fpx);
   t.fpy = __ldg(&cd->fpy);
+  t.fxb = __ldg(&cd->fxb);
   return t;
 }
 
@@ -757,6 +758,21 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
 
   const FT* __restrict__ fin = static_cast<const FT*>(a.f_in) + t.f_off;
   FT* __restrict__ fout = static_cast<FT*>(a.f_out) + t.f_off;
+  // f layout. Blocked (equilibrium g, all but the TMA kernel): population l of cell
+  // (x, y, z) at fz(z) + fy(y) + fx(x) + l*32, with fz = z*PS, fy = y*RS,
+  // fx = (x/32)*Q*32 + x%32. Per thread the x and y terms of a cell and of its pull sources
+  // (x -+ 1, y -+ 1, with periodic wrap) are fixed; per plane the z terms are uniform.
+  // Plain (stored g, and 64-bit offsets: those kernels have no registers to spare for the
+  // terms): population l at l*n + cell index.
+  constexpr bool kBlocked = EQ && !kTma && !kWide;
+  const IT RS = static_cast<IT>(t.fxb) * (QF * 32);
+  const IT PS = RS * ny;
+  auto fxof = [](int xs) -> IT { return static_cast<IT>(xs >> 5) * (QF * 32) + (xs & 31); };
+  const IT fx0 = kBlocked ? fxof(x) : 0, fxm = kBlocked ? fxof(xm) : 0;
+  const IT fxp = kBlocked ? fxof(xp) : 0;
+  const IT fy0 = kBlocked ? static_cast<IT>(y) * RS : 0;
+  const IT fym = kBlocked ? static_cast<IT>(y == 0 ? ny - 1 : y - 1) * RS : 0;
+  const IT fyp = kBlocked ? static_cast<IT>(y == ny - 1 ? 0 : y + 1) * RS : 0;
   const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
   GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
   const int* __restrict__ rest_in = EQ ? nullptr : a.rest_in + t.cell_off;
@@ -880,15 +896,31 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         tma_issue_plane<FT>(*pipe, pipe->buf + st * Box::kStageBytes, pipe->mbar + st, t.xt,
                             t.yt, z + 2, nz, t.bc, t.fgx);
     } else if (work) {
-      fr[0] = S::fload(fin + idx);
-      // 32-bit: one signed offset; 64-bit: the base pointer first (cheaper there).
-      auto pull = [&](auto LC) {
+      const IT fz0 = static_cast<IT>(z) * PS;
+      // this cell's population 0
+      const FT* __restrict__ fc = kBlocked ? fin + (fz0 + fy0 + fx0) : fin + idx;
+      // the stride between populations
+      constexpr int kLS = kBlocked ? 32 : 0;
+      const IT ls = kBlocked ? static_cast<IT>(kLS) : n;
+      fr[0] = S::fload(fc);
+      // Population L of source cell x - c_L. Blocked: its x, y and z terms, then L*32 as an
+      // immediate offset. Plain: L*n + cell (32-bit: one signed offset; 64-bit: the base
+      // pointer first, cheaper there).
+      auto pull = [&](auto LC, IT fzm, IT fzp) {
         constexpr int L = decltype(LC)::value;
-        const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
-                      src_of<cx(L)>(xm, x, xp);
-        if constexpr (kWide) fr[L] = S::fload(fin + L * n + s);
-        else fr[L] = S::fload(fin + (L * n + s));
+        if constexpr (kBlocked) {
+          const IT s = src_of<cz(L)>(fzm, fz0, fzp) + src_of<cy(L)>(fym, fy0, fyp) +
+                       src_of<cx(L)>(fxm, fx0, fxp);
+          fr[L] = S::fload(fin + s + L * kLS);
+        } else {
+          const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
+                        src_of<cx(L)>(xm, x, xp);
+          if constexpr (kWide) fr[L] = S::fload(fin + L * n + s);
+          else fr[L] = S::fload(fin + (L * n + s));
+        }
       };
+      const IT fzm = static_cast<IT>(z == 0 ? nz - 1 : z - 1) * PS;
+      const IT fzp = static_cast<IT>(z == nz - 1 ? 0 : z + 1) * PS;
       if (blo || bhi) {
         // A wall plane: what left through the wall returns as the cell's own opposite
         // population.
@@ -896,15 +928,11 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
           constexpr int L = decltype(LC)::value;
           constexpr int O = opp(L);
           const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
-          if (bounce) {
-            if constexpr (kWide) fr[L] = S::fload(fin + O * n + idx);
-            else fr[L] = S::fload(fin + (O * n + idx));
-          } else {
-            pull(LC);
-          }
+          if (bounce) fr[L] = S::fload(fc + O * ls);
+          else pull(LC, fzm, fzp);
         });
       } else {
-        static_for<1, QF>(pull);
+        static_for<1, QF>([&](auto LC) { pull(LC, fzm, fzp); });
       }
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
@@ -1114,10 +1142,18 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         if (ghosts) f_ghosts<L>(fout, fn, x, y, z, nx, ny, t.fgx, t.fpx, t.fpy, v);
       });
     } else {
-      static_for<0, QF>([&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        fout[L * n + idx] = S::template f_put<L>(fo[L]);
-      });
+      if constexpr (kBlocked) {
+        FT* __restrict__ fc = fout + (static_cast<IT>(z) * PS + fy0 + fx0);
+        static_for<0, QF>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          fc[L * 32] = S::template f_put<L>(fo[L]);
+        });
+      } else {
+        static_for<0, QF>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          fout[L * n + idx] = S::template f_put<L>(fo[L]);
+        });
+      }
     }
 
     if constexpr (BGK) {
@@ -1273,10 +1309,14 @@ __global__ void k_init(const InitArgs a) {
   }
   FT* f0 = static_cast<FT*>(a.f0) + cd->f_off;
   FT* f1 = static_cast<FT*>(a.f1) + cd->f_off;
-  // f layout (plain: fidx = idx, fn = n; padded: ghost columns and rows, kept periodic).
-  const long long fn = cd->fn;
+  // f layout: blocked (population stride 32 within a 32-cell x block), or padded (ghost
+  // columns and rows, kept periodic; the TMA update).
+  const int fxb = cd->fxb;
+  const long long fn = fxb ? 32 : cd->fn;
   const long long fidx =
-      (static_cast<long long>(z) * cd->fpy + y + (cd->fgx ? 1 : 0)) * cd->fpx + x + cd->fgx;
+      fxb ? ((static_cast<long long>(z) * ny + y) * fxb + (x >> 5)) * (QF * 32) + (x & 31)
+          : (static_cast<long long>(z) * cd->fpy + y + (cd->fgx ? 1 : 0)) * cd->fpx + x +
+                cd->fgx;
   const bool fghost = cd->fgx != 0 && !ref;
   const bool ratio = cd->drho != 0.f;
   GT* g0 = static_cast<GT*>(a.g0) + cd->g_off;

@@ -27,14 +27,18 @@ struct CaseDesc {
   int plane0;                             // first tile-plane index of this case
   long long ncell;     // nx*ny*nz
   long long cell_off;  // offset of the case's cells in per-cell arrays (phi, rest, macros)
-  long long f_off;     // element offset of the case's 19*ncell f values
+  long long f_off;     // element offset of the case's f values
   long long g_off;     // element offset of the case's 18*ncell moving g values
-  // f layout: element (l, x, y, z) at f_off + l*fn + (z*fpy + y + (fgx ? 1 : 0))*fpx + x + fgx.
-  // Plain: fgx 0, fpx nx, fpy ny, fn ncell. Padded (the TMA update): fgx ghost columns
-  // (16 bytes) on each side of a row and one ghost row on each side of a plane, which hold
-  // the periodic images of the opposite edge.
+  // f layout, blocked (fxb > 0: equilibrium g with 32-bit offsets, not the TMA update): fxb
+  // blocks of 32 cells in x per row, each holding its Q populations as runs of 32 values:
+  //   element (l, x, y, z) at f_off + ((z*ny + y)*fxb + x/32)*Q*32 + l*32 + x%32,
+  // so population l of a cell sits a fixed l*32 elements after its population 0.
+  // Otherwise element (l, x, y, z) at f_off + l*fn + (z*fpy + y + (fgx ? 1 : 0))*fpx + x +
+  // fgx. Plain (stored g, 64-bit offsets): fgx 0, fpx nx, fpy ny, fn ncell. Padded (the
+  // TMA update): fgx ghost columns (32 bytes) on each side of a row and one ghost row on
+  // each side of a plane, which hold the periodic images of the opposite edge.
   long long fn;
-  int fgx, fpx, fpy, pad1;
+  int fgx, fpx, fpy, fxb;
   float omega;         // 1/tau
   float omega_g;       // 1/tau_g
   float sigma;
