@@ -1020,17 +1020,34 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
     float rho = m0, jx = 0.f, jy = 0.f, jz = 0.f;
     float sxx = m2, syy = m2, szz = m2, sxy = 0.f, sxz = 0.f, syz = 0.f;
-    static_for<0, QF>([&](auto LC) {
-      constexpr int L = decltype(LC)::value;
-      const float v = f[L];
-      rho += v;
-      if constexpr (cx(L) != 0) { jx += cx(L) * v; sxx += v; }
-      if constexpr (cy(L) != 0) { jy += cy(L) * v; syy += v; }
-      if constexpr (cz(L) != 0) { jz += cz(L) * v; szz += v; }
-      if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * v;
-      if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
-      if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
-    });
+    if constexpr (EQ) {
+      // Opposite pairs (l odd, l + 1): their sum feeds rho and the second moments, their
+      // difference the momentum (about 30 % fewer adds than population by population).
+      rho += f[0];
+      static_for<0, (QF - 1) / 2>([&](auto KC) {
+        constexpr int L = 2 * decltype(KC)::value + 1;
+        const float sp = f[L] + f[L + 1], dm = f[L] - f[L + 1];
+        rho += sp;
+        if constexpr (cx(L) != 0) { jx += cx(L) * dm; sxx += sp; }
+        if constexpr (cy(L) != 0) { jy += cy(L) * dm; syy += sp; }
+        if constexpr (cz(L) != 0) { jz += cz(L) * dm; szz += sp; }
+        if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * sp;
+        if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * sp;
+        if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * sp;
+      });
+    } else {
+      static_for<0, QF>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        const float v = f[L];
+        rho += v;
+        if constexpr (cx(L) != 0) { jx += cx(L) * v; sxx += v; }
+        if constexpr (cy(L) != 0) { jy += cy(L) * v; syy += v; }
+        if constexpr (cz(L) != 0) { jz += cz(L) * v; szz += v; }
+        if constexpr (cx(L) * cy(L) != 0) sxy += (cx(L) * cy(L)) * v;
+        if constexpr (cx(L) * cz(L) != 0) sxz += (cx(L) * cz(L)) * v;
+        if constexpr (cy(L) * cz(L) != 0) syz += (cy(L) * cz(L)) * v;
+      });
+    }
     float ux, uy, uz, pxx, pyy, pzz, pxy, pxz, pyz, inv_rp = 0.f, rp = 1.f;
     if constexpr (kRatio) {
       // DensityRatio: velocity-based pressure formulation (Zu and He 2013; Fakhari et al.
