@@ -123,24 +123,27 @@ struct Solver {
   int ratio = 0;           // density-ratio model
   int wide = 0;            // some case needs 64-bit f offsets
   bool padded = false;     // f in the padded layout of the TMA collide
-  bool push = false;       // records not stored: the collide kernel writes the next phi
+  bool push = false;       // the collide kernel writes the next phi (all but the TMA kernel)
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
   mcb::CaseDesc* d_cases = nullptr;
   void* jbuf = nullptr;
   void* f[2] = {nullptr, nullptr};
   void* g[2] = {nullptr, nullptr};
+  // g rest population: stored g without push; with push only the first update's phi
+  // kernel reads one (the init's)
   int* rest[2] = {nullptr, nullptr};
-  // phi, Q2.30: two buffers alternate; the push mode rotates three (current, next,
-  // cleared for the one after)
-  int* p[3] = {nullptr, nullptr, nullptr};
+  // phi, Q2.30: two buffers alternate; the push mode rotates three (current, next, cleared
+  // for the one after) or, with stored g, four (the previous one, whose split the 16-bit g
+  // decode needs)
+  int* p[4] = {nullptr, nullptr, nullptr, nullptr};
   float* macros = nullptr;
   float* stage = nullptr;
   mcb::DiagPartial* partials = nullptr;
   mcb::DiagPartial* result = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaGraphExec_t graph[6] = {};  // per (f parity, phi slot) at the start of the graph
+  cudaGraphExec_t graph[8] = {};  // per (f parity, phi slot) at the start of the graph
   int graph_steps = 16;
   int ntiles = 0, zchunk = 16;
   int balanced = 1, phi_balanced = 0, planes = 0, grid_phi = 0, grid_collide = 0;
@@ -156,8 +159,8 @@ struct Solver {
     return MCB_OK;
   }
 
-  int nphi() const { return push ? 3 : 2; }
-  int graph_key() const { return parity * 3 + pk; }
+  int nphi() const { return push ? (gmode == mcb::kGEquil ? 3 : 4) : 2; }
+  int graph_key() const { return parity * 4 + pk; }
 
   void drop_graphs() {
     for (auto& ge : graph)
@@ -178,8 +181,10 @@ struct Solver {
       f[i] = g[i] = nullptr;
       rest[i] = p[i] = nullptr;
     }
-    cudaFree(p[2]);
-    p[2] = nullptr;
+    for (int i = 2; i < 4; ++i) {
+      cudaFree(p[i]);
+      p[i] = nullptr;
+    }
     cudaFree(macros);
     cudaFree(err);
     err = nullptr;
@@ -389,19 +394,18 @@ struct Solver {
     const size_t fb = f_bytes();
     const size_t gb = static_cast<size_t>(cells_total) * 18 * pop_bytes(storage);
     const size_t cb = static_cast<size_t>(cells_total) * sizeof(int);
+    // Every collide kernel but the TMA one writes the next phi itself; the TMA one keeps
+    // (phi, J) records and the phi kernel.
+    push = !padded;
     for (int i = 0; i < 2; ++i) {
       MCB_CU(cudaMalloc(&f[i], fb));
       if (padded) MCB_CU(cudaMemset(f[i], 0, fb));  // ghost columns nothing reads stay 0
       if (gmode != mcb::kGEquil) {
         MCB_CU(cudaMalloc(&g[i], gb));
-        MCB_CU(cudaMalloc(&rest[i], cb));
+        if (!push || i == 0) MCB_CU(cudaMalloc(&rest[i], cb));
       }
-      MCB_CU(cudaMalloc(&p[i], cb));
     }
-    // (phi, J) records: with full g relaxation every collide kernel but the TMA one writes
-    // the next phi itself; the TMA one keeps the records and the phi kernel.
-    push = gmode == mcb::kGEquil && !padded;
-    if (push) MCB_CU(cudaMalloc(&p[2], cb));
+    for (int i = 0; i < nphi(); ++i) MCB_CU(cudaMalloc(&p[i], cb));
     if (gmode == mcb::kGEquil && !push)
       MCB_CU(cudaMalloc(&jbuf, static_cast<size_t>(cells_total) * sizeof(float4)));
     MCB_CU(cudaMalloc(&macros, static_cast<size_t>(cells_total) * 5 * sizeof(float)));
@@ -523,7 +527,7 @@ struct Solver {
     // phi into the current buffer and the one diagnostics read; push: the next one cleared
     a.p0 = p[pk];
     a.p1 = p[(pk + nphi() - 1) % nphi()];
-    a.p_zero = push ? p[(pk + 1) % 3] : nullptr;
+    a.p_zero = push ? p[(pk + 1) % nphi()] : nullptr;
     a.macros = macros;
     a.cells_total = cells_total;
     a.gmode = gmode;
@@ -554,10 +558,10 @@ struct Solver {
     a.g_out = g[parity ^ 1];
     a.rest_in = rest[parity];
     a.rest_out = rest[parity ^ 1];
-    a.p_prev = p[(pk + 1) % nphi()];
+    a.p_prev = p[(pk + nphi() - 1) % nphi()];
     a.p_cur = p[pk];
-    a.p_next = push ? p[(pk + 1) % 3] : nullptr;
-    a.p_zero = push ? p[(pk + 2) % 3] : nullptr;
+    a.p_next = push ? p[(pk + 1) % nphi()] : nullptr;
+    a.p_zero = push ? p[(pk + 2) % nphi()] : nullptr;
     a.macros = with_macros ? macros : nullptr;
     a.j = jbuf;
     a.cells_total = cells_total;
@@ -567,7 +571,13 @@ struct Solver {
 
   // Equilibrium storage has no populations before the first collision: its first update
   // takes phi from the init and runs only the collide kernel.
-  bool skips_phi() const { return gmode == mcb::kGEquil && (push || first); }
+  // The phi kernel: equilibrium g runs it only without push and after the first update
+  // (the init's phi starts it); stored g without push on every update, with push on the
+  // first one only (its phi is the pulled sum of the init's populations, as every later
+  // phi is the pushed sum of the collided ones).
+  bool skips_phi() const {
+    return gmode == mcb::kGEquil ? (push || first) : (push && !first);
+  }
 
   // The phi stage of an update: the phi kernel, or nothing (push, first equilibrium update).
   int launch_phi_stage(const mcb::StepArgs& a) {
@@ -712,7 +722,7 @@ struct Solver {
       if (jbuf) v.push_back({jbuf, n * sizeof(float4)});
     } else {
       v.push_back({g[parity], n * 18 * pop_bytes(storage)});
-      v.push_back({rest[parity], n * sizeof(int)});
+      if (rest[parity]) v.push_back({rest[parity], n * sizeof(int)});
     }
     for (int i = 0; i < nphi(); ++i) v.push_back({p[i], n * sizeof(int)});
     v.push_back({macros, n * 5 * sizeof(float)});
@@ -1161,7 +1171,7 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     cudaFree(ms);
   };
   if (cudaMalloc(&fs, fb) != cudaSuccess || (gb && cudaMalloc(&gs, gb) != cudaSuccess) ||
-      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 12) != cudaSuccess ||
+      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 16) != cudaSuccess ||
       cudaMalloc(&ms, n * 20) != cudaSuccess) {
     free_all();
     return fail(MCB_ERR_ALLOC, "autotune: no room for a state copy");
@@ -1178,14 +1188,14 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     if (!restore) {
       if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
       if (e == cudaSuccess && gb) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
-      if (e == cudaSuccess && !eq) e = cp(rs, s.rest[par], n * 4);
+      if (e == cudaSuccess && s.rest[par]) e = cp(rs, s.rest[par], n * 4);
       for (int i = 0; i < s.nphi(); ++i)
         if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + i * n * 4, s.p[i], n * 4);
       if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
     } else {
       if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
       if (e == cudaSuccess && gb) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
-      if (e == cudaSuccess && !eq) e = cp(s.rest[par], rs, n * 4);
+      if (e == cudaSuccess && s.rest[par]) e = cp(s.rest[par], rs, n * 4);
       for (int i = 0; i < s.nphi(); ++i)
         if (e == cudaSuccess) e = cp(s.p[i], static_cast<char*>(ps) + i * n * 4, n * 4);
       if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);

@@ -654,14 +654,15 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     for (int k = 0; k < KPF; ++k)
       if (tid + k * NT < PP) d[tid + k * NT] = __int2float_rn(pre[k]) * kInvQ30;
   };
-  // kPush: the collide kernel writes the next update's phi itself. Each cell s pushes its
-  // 19 exact Q2.30 populations q_l = w_l(P_s) + m_l c_l.J'_s to their consumers
-  // s + c_l (the same integers the record rebuild pulls): inside the tile through a
-  // 4-plane shared ring of integer sums (tile + halo 1), flushed to global memory with
-  // integer atomic adds once a target plane is complete. Integer sums do not depend on the
-  // order, so the result is the record rebuild's, bit for bit, with no records and no phi
+  // kPush (every kernel but the TMA one): the collide kernel writes the next update's phi
+  // itself. Each cell s pushes its 19 exact Q2.30 populations to their consumers s + c_l:
+  // with equilibrium g q_l = w_l(P_s) + m_l c_l.J'_s (the integers the record rebuild
+  // pulls), with stored g the integers it stores and the rest part P_s - sum q. Inside the
+  // tile they go through a 4-plane shared ring of integer sums (tile + halo 1), flushed to
+  // global memory with integer atomic adds once a target plane is complete. Integer sums do
+  // not depend on the order, so the next phi is the pulled sum, bit for bit, with no phi
   // kernel.
-  constexpr bool kPush = EQ && !kTma;
+  constexpr bool kPush = !kTma;
   __shared__ int sacc[kPush ? 4 : 1][kPush ? HP : 1];
   int* __restrict__ pnext = kPush ? a.p_next + t.cell_off : nullptr;
   int* __restrict__ pzero = kPush ? a.p_zero + t.cell_off : nullptr;
@@ -775,8 +776,8 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   const IT fyp = kBlocked ? static_cast<IT>(y == ny - 1 ? 0 : y + 1) * RS : 0;
   const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
   GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
-  const int* __restrict__ rest_in = EQ ? nullptr : a.rest_in + t.cell_off;
-  int* __restrict__ rest_out = EQ ? nullptr : a.rest_out + t.cell_off;
+  const int* __restrict__ rest_in = (EQ || kPush) ? nullptr : a.rest_in + t.cell_off;
+  int* __restrict__ rest_out = (EQ || kPush) ? nullptr : a.rest_out + t.cell_off;
   float4* __restrict__ jout = EQ ? static_cast<float4*>(a.j) + t.cell_off : nullptr;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
@@ -800,21 +801,21 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   // Pushes the populations of source cell (x, y, z), phi P and integer flux J', into the
   // shared ring: q_l to target plane z + cz(l), the rest part and populations bounced at a
   // z wall to the cell itself.
-  auto push = [&](int z, int P, const JQ& jq) {
+  // Adds population L of the cell, value(L), to its consumer in the ring: L = 1..18 first,
+  // then the rest part (value(0)), so a value may depend on the ones before it.
+  auto push_values = [&](int z, auto&& value) {
     if constexpr (kPush) {
       const int o = (ty + 1) * HX + tx + 1;
       int* s0 = &sacc[(z + 8) & 3][o];
       int* sm = &sacc[(z + 7) & 3][o];
       int* sp = &sacc[(z + 9) & 3][o];
-      const int wfc = wsplit_face(P), wed = wsplit_edge_of_face(wfc);
-      atomicAdd(s0, P - 6 * wfc - 12 * wed);  // the rest part
       if (walls && (z == 0 || z == nz - 1)) {
         // A wall plane: what leaves through the wall returns to the cell itself.
         const bool blo = z == 0, bhi = z == nz - 1;
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
           constexpr int D = cy(L) * HX + cx(L);
-          const int q = (L <= 6 ? wfc : wed) + qj<L>(jq);
+          const int q = value(LC);
           const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
           int* tgt = cz(L) < 0 ? sm + D : (cz(L) > 0 ? sp + D : s0 + D);
           atomicAdd(bounce ? s0 : tgt, q);
@@ -825,10 +826,20 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
           constexpr int L = decltype(LC)::value;
           constexpr int D = cy(L) * HX + cx(L);
           int* b = cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0);
-          atomicAdd(b + D, (L <= 6 ? wfc : wed) + qj<L>(jq));
+          atomicAdd(b + D, value(LC));
         });
       }
+      atomicAdd(s0, value(std::integral_constant<int, 0>{}));
     }
+  };
+  // Equilibrium g of phi P and integer flux J'.
+  auto push = [&](int z, int P, const JQ& jq) {
+    const int wfc = wsplit_face(P), wed = wsplit_edge_of_face(wfc);
+    push_values(z, [&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      if constexpr (L == 0) return P - 6 * wfc - 12 * wed;  // the rest part
+      else return (L <= 6 ? wfc : wed) + qj<L>(jq);
+    });
   };
 
   // Normals one plane ahead (kAhead): each plane takes one barrier, after which the normals
@@ -958,12 +969,13 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       } else if constexpr (EQ) {
         jout[idx] = make_float4(__int_as_float(pc), __int_as_float(0), __int_as_float(0),
                                 __int_as_float(0));
-      } else {
+      }
+      if constexpr (!EQ) {
         static_for<1, kQ>([&](auto LC) {
           constexpr int L = decltype(LC)::value;
           gout[(L - 1) * ng + idx] = S::template g_shell<L>(pc);
         });
-        rest_out[idx] = S::rest_shell(pc);
+        if constexpr (!kPush) rest_out[idx] = S::rest_shell(pc);
       }
       if (a.macros) {
         const long long T = a.cells_total, o = t.cell_off + idx;
@@ -1205,15 +1217,28 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         jout[idx] = make_float4(__int_as_float(pc), __int_as_float(jq.x), __int_as_float(jq.y),
                                 __int_as_float(jq.z));
     } else {
+      // Stored g: the 18 moving populations as stored (exact Q2.30 integers q) and the rest
+      // part, the exact remainder P - sum q. In push mode they also go to their consumers'
+      // next phi, and the rest part is not stored (no phi kernel reads it).
       int sumq = 0;
       const GSplit sp = S::g_split(pc);
-      static_for<1, kQ>([&](auto LC) {
+      auto gval = [&](auto LC) {
         constexpr int L = decltype(LC)::value;
-        int q;
-        gout[(L - 1) * ng + idx] = S::template g_put<L>(go[L], sp, q);
-        sumq += q;
-      });
-      rest_out[idx] = S::rest_store(pc, sumq);
+        if constexpr (L == 0) {
+          return pc - sumq;
+        } else {
+          int q;
+          gout[(L - 1) * ng + idx] = S::template g_put<L>(go[L], sp, q);
+          sumq += q;
+          return q;
+        }
+      };
+      if constexpr (kPush) {
+        push_values(z, gval);
+      } else {
+        static_for<1, kQ>(gval);
+        rest_out[idx] = S::rest_store(pc, sumq);
+      }
     }
 
     if (a.macros) {
@@ -1307,8 +1332,9 @@ __global__ void k_init(const InitArgs a) {
                              z == nz - 1);
   const bool eq = a.gmode == kGEquil;
   const float phi_self = a.phi[idx];
-  // Equilibrium storage skips k_phi on the first update, so its phi starts here; the
-  // reference's shell phi starts at 0 (src/var.cu:86).
+  // Equilibrium g: the first update takes its phi from here (no phi kernel runs before
+  // it); the reference's shell phi starts at 0 (src/var.cu:86). Stored g: the first
+  // update's phi kernel sums the populations written below.
   const int P = (eq && shell) ? 0 : __float2int_rn(phi_self * kQ30);
   a.p0[co + idx] = P;
   a.p1[co + idx] = P;
@@ -1384,7 +1410,7 @@ __global__ void k_init(const InitArgs a) {
     if (eq) {
       // no g populations are stored
     } else if constexpr (L == 0) {
-      a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
+      if (a.rest0) a.rest0[co + idx] = S::rest_init(wf(0) * phi_self, P);
     } else if constexpr (L < kQ) {  // g is D3Q19
       const float geq = wf(L) * a.phi[ci] * (1.0f + 3.0f * cu);
       int q;
