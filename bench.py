@@ -47,13 +47,16 @@ TMA_VARIANT = 4
 def g_storage(cfg, variant: int = -1) -> str:
     """How the phase field crosses an update.
       push         g at equilibrium (tau_g = 1, the default): the collide kernel adds each
-                   cell's integer populations into the next phi; no phi kernel
+                   cell's integer populations into the next phi; no g is stored
       records      the same g, with a 16-byte (P, J) record per cell and the phi kernel
                    (the TMA-staged collide)
-      populations  stored g populations (tau_g != 1) and the phi kernel"""
+      populations  g stored (MCB_G_POPULATIONS at tau_g = 1) and pushed into the next phi
+      bgk          g stored and relaxed with tau_g != 1 (pulled and stored), pushed likewise"""
     import mcb
 
-    if cfg.tau_g != 1.0 or cfg.g_mode == mcb.G_POPULATIONS:
+    if cfg.tau_g != 1.0:
+        return "bgk"
+    if cfg.g_mode == mcb.G_POPULATIONS:
         return "populations"
     return "records" if variant == TMA_VARIANT else "push"
 
@@ -64,20 +67,22 @@ def bytes_per_lu(cfg, storage: str, variant: int = -1) -> tuple[int, int, int]:
       push         collide: f in and out (Q populations), phi in, the next phi (integer
                    atomics into L2, counted once), the phi buffer after next cleared (4 B)
       records      phi kernel: the record in, phi out; collide: f in and out, phi in, record out
-      populations  phi kernel: 18 g and the rest in, phi out, and the previous phi in with
-                   16-bit storage (the base of its deviation form); collide: f in and out,
-                   phi in, 18 g and the rest out"""
+      populations  collide: as push, and the 18 moving g out
+      bgk          collide: as push, the 18 moving g in and out, and with 16-bit storage the
+                   previous phi in (the base of the deviation form)"""
     pb = 4 if storage == "f32" else 2
     q = 27 if cfg.velocity_set == 27 else 19
     f = 2 * q * pb
+    push = f + 4 + 4 + 4
     gs = g_storage(cfg, variant)
     if gs == "push":
-        ph, col = 0, f + 4 + 4 + 4
+        ph, col = 0, push
     elif gs == "records":
         ph, col = 16 + 4, f + 4 + 16
+    elif gs == "populations":
+        ph, col = 0, push + 18 * pb
     else:
-        ph = 18 * pb + 4 + 4 + (4 if storage != "f32" else 0)
-        col = f + 4 + 18 * pb + 4
+        ph, col = 0, push + 2 * 18 * pb + (4 if storage != "f32" else 0)
     return ph, col, ph + col
 
 
@@ -85,8 +90,9 @@ def footprint_bytes(cells: int, storage: str, gs: str, q: int = 19) -> int:
     """Device bytes of one solver handle: f ping-pong, g state, phi buffers, macros,
     host-upload staging."""
     pb = 4 if storage == "f32" else 2
-    g = {"push": cells * 4, "records": cells * 16}.get(gs, 2 * cells * (18 * pb + 4))
-    return 2 * cells * q * pb + g + 2 * cells * 4 + cells * 5 * 4 + cells * 4 * 4
+    g = {"push": 3 * cells * 4, "records": cells * 16 + 2 * cells * 4}.get(
+        gs, 2 * cells * 18 * pb + cells * 4 + 4 * cells * 4)
+    return 2 * cells * q * pb + g + cells * 5 * 4 + cells * 4 * 4
 
 
 def dist_env():
@@ -496,9 +502,10 @@ def main():
                      "update_achieved": update_achieved, "update_frac": update_achieved / hbm,
                      "update_bytes_per_lu": upd_b,
                      "kernel_ms": {"phi_stage": phi_ms / args.steps, "k_collide": col_ms / args.steps}},
-        # push: one collide launch per update; else the phi kernel and the collide kernel
         "roofline_mlups_fg": metric_roofline,
-        "gpu_launches": (1 if gs == "push" else 2) * args.steps,
+        # one collide launch per update, but with the TMA records: the phi kernel and the
+        # collide kernel
+        "gpu_launches": (2 if gs == "records" else 1) * args.steps,
         "clocks": clk.summary(),
         "mass_q30_finite": bool(diag["finite"]),
     }
