@@ -204,7 +204,8 @@ int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
  * next update reads:
  *   - the f populations, and the g populations (or the (phi, J) records of the TMA
  *     variant) where g is stored;
- *   - every phi buffer (two, or three in the default equilibrium g mode);
+ *   - every phi buffer (two with the TMA variant, three with equilibrium g, four with
+ *     stored g);
  *   - the fields of the latest update;
  *   - the update counter, the buffer parity and the buoyancy reference;
  * together with the configuration. mcb_checkpoint_load restores them into a handle created
