@@ -870,6 +870,8 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     const int zp = (z == nz - 1 ? 0 : z + 1) * nxy;
     const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
 
+    // This cell's phi (read now, used after the barrier).
+    const int pc = active ? __ldg(pcur + idx) : 0;
     // Pull the 19 f populations (issued before the barriers to overlap their latency).
     FT fr[QF];
     if constexpr (kTma) {
@@ -956,7 +958,6 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
     if (!active) continue;
 
-    const int pc = __ldg(pcur + idx);
     if constexpr (kPush) pzero[idx] = 0;  // the next update accumulates into it
     if (shell) {
       // Reference shell cell: rest-equilibrium inflow g = W_l * phi_b
