@@ -373,8 +373,13 @@ def test_field_dumps_are_read_by_post_file_treat_names(tmp_path):
         assert np.array_equal(raw.reshape(want[name].shape), want[name]), name
 
 
-def test_autotune_restores_the_state():
-    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(32, 32, 32), noise=1e-3)
+@pytest.mark.parametrize("tau_g,storage", [(1.0, mcb.STORE_F32), (0.8, mcb.STORE_F32),
+                                           (0.8, mcb.STORE_F16)])
+def test_autotune_restores_the_state(tau_g, storage):
+    """Stored g keeps four phi buffers (the previous one is the base of the 16-bit g
+    decode): every one of them must come back after the trials."""
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(32, 32, 32), tau_g=tau_g, noise=1e-3)
+    cfg.storage = storage
     ref = gpu_run(cfg, phi, u, steps=20)
     with mcb.Solver(cfg) as s:
         s.set_fields(phi, *u)
