@@ -706,19 +706,15 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   };
 
   // Phi-plane offset of normals point i (the same on every plane), -1 where (reference
-  // mode) the point is on or beyond the shell in x or y and its normal is 0. The 32-bit
-  // offset kernels read them from a table filled here (the rings fill after the barrier
-  // that follows); the 64-bit ones compute them per plane (measured 3 % faster there).
-  constexpr bool kCenTab = !kWide;
-  auto center = [&](int i) {
+  // mode) the point is on or beyond the shell in x or y and its normal is 0: a table
+  // filled here, once per run (the rings fill after the barrier that follows).
+  __shared__ int scen[HP];
+  for (int i = tid; i < HP; i += NT) {
     const int hx = i % HX, hy = i / HX;
     const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
     const bool zero = ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1);
-    return zero ? -1 : (hy + 1) * PX + hx + 1;
-  };
-  __shared__ int scen[kCenTab ? HP : 1];
-  if constexpr (kCenTab)
-    for (int i = tid; i < HP; i += NT) scen[i] = center(i);
+    scen[i] = zero ? -1 : (hy + 1) * PX + hx + 1;
+  }
   // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72).
   auto normals = [&](int zp) {
     const float* pm = sphi[(zp + 4) % 5];
@@ -727,7 +723,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     float(*dst)[HP] = snrm[(zp + 4) % 4];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
     for (int i = tid; i < HP; i += NT) {
-      const int c = kCenTab ? scen[i] : center(i);
+      const int c = scen[i];
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
       if (c >= 0 && !zshell) {
         float gxs = 0.f, gys = 0.f, gzs = 0.f;
@@ -842,25 +838,22 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     });
   };
 
-  // Normals one plane ahead (kAhead): each plane takes one barrier, after which the normals
-  // of plane z+2 go into the fourth ring slot while the collision of plane z reads planes
-  // z-1 .. z+1. Otherwise (the 64-bit-offset kernels, where it measured 8 % slower at
-  // 448^3 FP16) the normals of plane z+1 sit between two barriers.
-  constexpr bool kAhead = !kWide;
-  constexpr int kLead = kAhead ? 1 : 0;
-  // Prologue: phi planes zb-2 .. zb+1+kLead, normals zb-1 .. zb+kLead.
-  for (int zpl = t.zb - 2; zpl <= t.zb + 1 + kLead; ++zpl) {
+  // Normals one plane ahead: each plane takes one barrier, after which the normals of
+  // plane z+2 go into the fourth ring slot while the collision of plane z reads planes
+  // z-1 .. z+1.
+  // Prologue: phi planes zb-2 .. zb+2, normals zb-1 .. zb+1.
+  for (int zpl = t.zb - 2; zpl <= t.zb + 2; ++zpl) {
     issue(zpl);
     commit(zpl);
   }
-  issue(t.zb + 2 + kLead);
+  issue(t.zb + 3);
   __syncthreads();
-  for (int zpl = t.zb - 1; zpl <= t.zb + kLead; ++zpl) normals(zpl);
-  if constexpr (kAhead) __syncthreads();
+  for (int zpl = t.zb - 1; zpl <= t.zb + 1; ++zpl) normals(zpl);
+  __syncthreads();
 
   for (int z = t.zb; z < t.ze; ++z) {
-    commit(z + 2 + kLead);
-    if (z + 3 + kLead <= t.ze + 1) issue(z + 3 + kLead);
+    commit(z + 3);
+    if (z + 4 <= t.ze + 1) issue(z + 4);
 
     const int zo = z * nxy;
     const int idx = x + yo + zo;
@@ -950,12 +943,7 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
     if (kPush && z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
-    if constexpr (kAhead) {
-      if (z + 2 <= t.ze) normals(z + 2);
-    } else {
-      normals(z + 1);
-      __syncthreads();
-    }
+    if (z + 2 <= t.ze) normals(z + 2);
     if (!active) continue;
 
     if constexpr (kPush) pzero[idx] = 0;  // the next update accumulates into it
