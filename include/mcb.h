@@ -5,9 +5,11 @@
  * (src/main.cu:74-190 of kreeyto/MULTIC-BUBBLE-CUDA):
  *   - g carries a conservative Allen-Cahn phase field phi;
  *   - f carries the flow, with regularized collision and He-style surface-tension forcing.
- * The ten launches of that loop (src/lbm.cu:5-461) become two fused sm_103a kernels per
- * update. The first pull-streams g and sums phi. The second computes normals, curvature,
- * force, moments, the regularized f collision and the g collision.
+ * The ten launches of that loop (src/lbm.cu:5-461) become one fused sm_103a kernel per
+ * update. It computes normals, curvature, force, moments, the regularized f collision and
+ * the g collision, pull-streams f, and adds each cell's exact integer g populations into
+ * the next update's phi (the pull-stream of g and the phi sum of the reference). Only the
+ * opt-in TMA variant, and the first update with stored g, run a separate phi kernel.
  *
  * Conventions:
  *   - Every call returns an int status: MCB_OK (0) or one of MCB_ERR_*. The reference
