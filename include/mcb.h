@@ -300,7 +300,7 @@ int  mcb_fill_phi_bubbles(int nx, int ny, int nz, int bc, float width,
 int  mcb_workload(int scenario, int case_index, uint64_t seed, double scale,
                   mcb_config* cfg, float* phi, float* ux, float* uy, float* uz);
 
-/* ---- batched cases: many independent cases of uneven size in one launch per phase ---- */
+/* ---- batched cases: many independent cases of uneven size in one launch per update ---- */
 
 /* All cases must share storage; each keeps its own size, bc, tau, sigma, ... */
 int  mcb_batch_create(const mcb_config* cases, int ncases, mcb_batch** out);

@@ -3,13 +3,8 @@
 // The reference runs ten launches per update (src/main.cu:79-178):
 //   phiCalc, gradCalc, curvatureCalc, momentiCalc, collisionFluid, collisionPhase,
 //   movingWallBC, streamingCalc, fgBoundary, boundaryConditions.
-// Between them it keeps 22 full-grid arrays in HBM. Here one update is two kernels:
+// Between them it keeps 22 full-grid arrays in HBM. Here one update is one kernel:
 //
-//   k_phi      pull-gathers the 19 g populations of every cell and sums them into phi.
-//              This is streamingCalc + phiCalc (src/lbm.cu:337-357, 5-26), plus the lagged
-//              shell copy of boundaryConditions (src/lbm.cu:403-425) in reference mode.
-//   k_phi_eq   the same when g is stored as one (phi, J) record per cell (full g
-//              relaxation, the default): it rebuilds the 18 pulled populations exactly.
 //   k_collide  marches a BX x BY column of cells through a z chunk. It keeps a 5-plane
 //              ring of phi (halo 2) and a 4-plane ring of normals (halo 1) in shared
 //              memory, the normals computed one plane ahead so that each plane takes one
@@ -20,20 +15,27 @@
 //                - the regularized f collision with He forcing (collisionFluid,
 //                  src/lbm.cu:233-288);
 //                - the g collision (collisionPhase, src/lbm.cu:290-329).
-//              Populations are stored post-collision at the colliding cell. The next
-//              update gathers them from x - c_l (pull streaming). In reference mode the
-//              shell cells write the rest-equilibrium inflow of fgBoundary
-//              (src/lbm.cu:365-401).
+//              f is stored post-collision at the colliding cell; the next update gathers
+//              it from x - c_l (pull streaming). The g populations, as exact Q2.30
+//              integers, are added straight into the next update's phi at x + c_l
+//              (streamingCalc + phiCalc, src/lbm.cu:337-357, 5-26), through a shared ring
+//              and integer atomics. In reference mode the shell cells write the
+//              rest-equilibrium inflow of fgBoundary (src/lbm.cu:365-401) and their next
+//              phi, the lagged copy of boundaryConditions (src/lbm.cu:403-425).
+//   k_phi      pull-gathers the 19 stored g populations of every cell and sums them into
+//              phi: the first update with stored g only (its phi comes from the init).
+//   k_phi_eq   the same when g is kept as one (phi, J) record per cell: the opt-in TMA
+//              variant only.
 //
-// HBM traffic per lattice update: f read and written once, plus either the 16-byte record
-// written once and read once (default) or g read and written once, plus 8 bytes of phi.
-// Nothing else reaches HBM: normals, curvature, force and moments live in registers and
-// shared memory.
+// HBM traffic per lattice update: f read and written once and 12 bytes of phi (read, the
+// next one accumulated, the one after cleared); with stored g, g written (and read when
+// it relaxes with tau_g != 1). Nothing else reaches HBM: normals, curvature, force and
+// moments live in registers and shared memory.
 //
-// phi is carried as Q2.30 fixed point. Every g collision writes the rest population as
-// the exact integer remainder. The 19 stored values of a cell therefore add up to its
-// phi exactly, and streaming and bounce-back are permutations. So the lattice sum of
-// phi is invariant to the last bit in periodic and walled domains.
+// phi is carried as Q2.30 fixed point. Every g collision makes the rest population the
+// exact integer remainder, so the 19 integers a cell sends add up to its phi exactly,
+// and streaming and bounce-back only move them. So the lattice sum of phi is invariant to
+// the last bit in periodic and walled domains.
 #pragma once
 
 #include <cuda.h>  // CUtensorMap
