@@ -1284,9 +1284,17 @@ __global__ void __launch_bounds__(kTmaBX * kTmaBY, kCollideWarpsPerSM * 32 / (kT
   }, a.balanced != 0);
 }
 
-// D3Q27 f: 32x8 tiles, two blocks of eight warps per SM (27 populations in flight).
+// D3Q27 f: 32x8 tiles, 27 populations in flight: two blocks of eight warps per SM
+// (128 registers). With equilibrium g, 16-bit storage and 32-bit offsets three blocks
+// (80 registers, a small spill) measured 9 % faster at 128 x 128 x 256; at FP32 they
+// measured 3 % slower, and the other forms spill three to five times as much.
 template <class S, int GM, bool kWide>
-__global__ void __launch_bounds__(256, 2) k_collide27(const StepArgs a) {
+constexpr int collide27_blocks() {
+  return (!std::is_same<typename S::FT, float>::value && GM == kGEquil && !kWide) ? 3 : 2;
+}
+template <class S, int GM, bool kWide>
+__global__ void __launch_bounds__(256, collide27_blocks<S, GM, kWide>())
+    k_collide27(const StepArgs a) {
   for_each_segment<32, 8, true>(
       a, [&](const Tile& t) { collide_segment<S, GM, 32, 8, false, kQ27, false, kWide>(a, t); }, a.balanced != 0);
 }
