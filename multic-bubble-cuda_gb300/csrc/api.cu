@@ -1160,7 +1160,8 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   const size_t n = static_cast<size_t>(s.cells_total);
   const bool eq = s.gmode == mcb::kGEquil;
   const size_t fb = s.f_bytes();
-  // Equilibrium storage keeps a (phi, J) record per cell in place of g and its rest.
+  // g state: stored populations, or with equilibrium g the (phi, J) records of the TMA
+  // variant (none in push mode).
   const size_t gb = eq ? (s.jbuf ? n * sizeof(float4) : 0) : n * 18 * pop_bytes(s.storage);
   void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
   auto free_all = [&]() {

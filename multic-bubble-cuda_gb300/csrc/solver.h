@@ -9,13 +9,14 @@ namespace mcb {
 enum Bc : int { kBcRef = 0, kBcPeriodic = 1, kBcWallsZ = 2 };
 enum Storage : int { kStF32 = 0, kStF16 = 1, kStBF16 = 2 };
 
-// How g crosses from one update to the next.
-//   kGPop:   19 stored populations, full relaxation (g* = geq).
-//   kGBgk:   19 stored populations, BGK relaxation with tau_g != 1.
-//   kGEquil: full relaxation stores only the Q2.30 phi and J = 3 phi u + sharp_c phi (1 - phi) n
-//            per cell, one 16-byte record. Each post-collision population is the
-//            equilibrium W_l (phi + c_l . J) of its source cell, so the next update rebuilds
-//            it from the source's record.
+// How g crosses from one update to the next. Every collide kernel but the TMA one adds
+// the post-collision populations, as exact Q2.30 integers, into the next update's phi.
+//   kGPop:   the 18 moving populations are also stored, full relaxation (g* = geq).
+//   kGBgk:   they are stored, and the next update pulls and relaxes them (tau_g != 1).
+//   kGEquil: full relaxation, nothing stored: each post-collision population is the
+//            equilibrium W_l (phi + c_l . J), J = 3 phi u + sharp_c phi (1 - phi) n, of its
+//            source cell. The TMA collide keeps phi and J as one 16-byte record per cell,
+//            from which its phi kernel rebuilds the populations.
 enum GMode : int { kGPop = 0, kGBgk = 1, kGEquil = 2 };
 
 // One case of a launch. A single-case handle has one entry. A batch has one entry per case,
