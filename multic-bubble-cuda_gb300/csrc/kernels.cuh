@@ -601,8 +601,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   constexpr int PX = BX + 4, PY = BY + 4, PP = PX * PY;  // phi plane, halo 2
   constexpr int HX = BX + 2, HY = BY + 2, HP = HX * HY;  // normals plane, halo 1
   constexpr int KPF = (PP + NT - 1) / NT;                // phi values per thread per plane
-  __shared__ float sphi[5][PP];
-  __shared__ float snrm[4][4][HP];  // nx, ny, nz, |grad phi| of four planes
+  static_assert(PX % 2 == 0 && HX % 2 == 0, "normals are computed for pairs of points in x");
+  __shared__ __align__(16) float sphi[5][PP];
+  __shared__ __align__(16) float snrm[4][4][HP];  // nx, ny, nz, |grad phi| of four planes
 
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int nxy = nx * ny;
@@ -707,44 +708,52 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     }
   };
 
-  // Phi-plane offset of normals point i (the same on every plane), -1 where (reference
-  // mode) the point is on or beyond the shell in x or y and its normal is 0: a table
-  // filled here, once per run (the rings fill after the barrier that follows).
+  // Phi-plane offset c of normals point i (the same on every plane), stored as -c - 1
+  // where (reference mode) the point is on or beyond the shell in x or y and its normal
+  // is 0: a table filled here, once per run (the rings fill after the barrier that
+  // follows).
   __shared__ int scen[HP];
   for (int i = tid; i < HP; i += NT) {
     const int hx = i % HX, hy = i / HX;
     const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
     const bool zero = ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1);
-    scen[i] = zero ? -1 : (hy + 1) * PX + hx + 1;
+    const int c = (hy + 1) * PX + hx + 1;
+    scen[i] = zero ? -c - 1 : c;
   }
   // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72).
+  // A thread takes two neighbouring points in x and computes both with packed FP32 pairs
+  // (each lane the same fused operations in the same order as one point alone). Their
+  // first point sits at an odd phi-plane offset, so the neighbours at x -+ 1 of the pair
+  // are aligned pairs in shared memory.
   auto normals = [&](int zp) {
     const float* pm = sphi[(zp + 4) % 5];
     const float* p0 = sphi[(zp + 5) % 5];
     const float* pp = sphi[(zp + 6) % 5];
     float(*dst)[HP] = snrm[(zp + 4) % 4];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
-    for (int i = tid; i < HP; i += NT) {
-      const int c = scen[i];
-      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (c >= 0 && !zshell) {
-        float gxs = 0.f, gys = 0.f, gzs = 0.f;
-        static_for<1, kQ>([&](auto LC) {
-          constexpr int L = decltype(LC)::value;
-          constexpr float w3 = 3.0f * wf(L);
-          const float v = nbr_of<cz(L)>(pm, p0, pp)[c + cy(L) * PX + cx(L)];
-          if constexpr (cx(L) != 0) gxs += (cx(L) * w3) * v;
-          if constexpr (cy(L) != 0) gys += (cy(L) * w3) * v;
-          if constexpr (cz(L) != 0) gzs += (cz(L) * w3) * v;
-        });
-        const float g2 = gxs * gxs + gys * gys + gzs * gzs;
-        const float fac = rsqrtf(fmaxf(g2, 1e-9f));
-        r = make_float4(gxs * fac, gys * fac, gzs * fac, g2 * fac);
-      }
-      dst[0][i] = r.x;
-      dst[1][i] = r.y;
-      dst[2][i] = r.z;
-      dst[3][i] = r.w;
+    for (int j = tid; 2 * j < HP; j += NT) {
+      const int e0 = scen[2 * j], e1 = scen[2 * j + 1];
+      const int c = e0 >= 0 ? e0 : -e0 - 1;  // the pair's first point; the second is c + 1
+      float2 gx = make_float2(0.f, 0.f), gy = gx, gz = gx;
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr float w3 = 3.0f * wf(L);
+        const float* q = nbr_of<cz(L)>(pm, p0, pp) + c + cy(L) * PX + cx(L);
+        const float2 v =
+            cx(L) != 0 ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
+        if constexpr (cx(L) != 0) gx = __ffma2_rn(make_float2(cx(L) * w3, cx(L) * w3), v, gx);
+        if constexpr (cy(L) != 0) gy = __ffma2_rn(make_float2(cy(L) * w3, cy(L) * w3), v, gy);
+        if constexpr (cz(L) != 0) gz = __ffma2_rn(make_float2(cz(L) * w3, cz(L) * w3), v, gz);
+      });
+      const float2 g2 = __ffma2_rn(gz, gz, __ffma2_rn(gy, gy, __fmul2_rn(gx, gx)));
+      float2 fac = make_float2(rsqrtf(fmaxf(g2.x, 1e-9f)), rsqrtf(fmaxf(g2.y, 1e-9f)));
+      // zero normals on the reference shell
+      if (zshell || e0 < 0) fac.x = 0.f;
+      if (zshell || e1 < 0) fac.y = 0.f;
+      reinterpret_cast<float2*>(dst[0])[j] = __fmul2_rn(gx, fac);
+      reinterpret_cast<float2*>(dst[1])[j] = __fmul2_rn(gy, fac);
+      reinterpret_cast<float2*>(dst[2])[j] = __fmul2_rn(gz, fac);
+      reinterpret_cast<float2*>(dst[3])[j] = __fmul2_rn(g2, fac);
     }
   };
 
