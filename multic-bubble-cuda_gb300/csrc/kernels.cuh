@@ -731,7 +731,12 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     const float* pp = sphi[(zp + 6) % 5];
     float(*dst)[HP] = snrm[(zp + 4) % 4];
     const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
-    for (int j = tid; 2 * j < HP; j += NT) {
+    // 16-bit relaxed g (the heaviest per-cell work, its g decode) hands the pairs out from
+    // the last thread down, away from the threads that take the second phi points of
+    // commit and the second ring positions of flush: 15 % faster there, 1-2 % slower in
+    // the other forms.
+    constexpr bool kTopDown = BGK && S::kDev;
+    for (int j = kTopDown ? NT - 1 - tid : tid; 2 * j < HP; j += NT) {
       const int e0 = scen[2 * j], e1 = scen[2 * j + 1];
       const int c = e0 >= 0 ? e0 : -e0 - 1;  // the pair's first point; the second is c + 1
       float2 gx = make_float2(0.f, 0.f), gy = gx, gz = gx;
