@@ -18,8 +18,10 @@ update reads and writes hold 638 MB.
             against the measured HBM copy bandwidth.
   cpu_baseline  the FP64 oracle (a restatement of the reference update) on the host cores.
 
---impl reference times the reference path on the host cores. The reference has no CPU
-implementation, so that path is the oracle port. --gpus N > 1 runs N independent replicas,
+--impl reference times the reference path on the host cores, on the same full-size workload.
+The reference has no CPU implementation, so that path is the oracle port; its initial field
+comes from the oracle-side generator (oracle/workload_port.py), so that arm loads no solver
+code. --gpus N > 1 runs N independent replicas,
 one per GPU; the path has no exchange step between cases.
 """
 from __future__ import annotations
@@ -42,6 +44,8 @@ sys.path.insert(0, str(REPO / "multic-bubble-cuda_gb300"))
 METRIC = "MLUPS and % HBM roofline; FP16-store vs FP32 at fixed Laplace-law error"
 SCENARIO, SEED = 2, 1
 TMA_VARIANT = 4
+# Population storage: the arithmetic is FP32 whatever the storage ("dtype" of the line).
+STORAGE_WORDS = {"f32": "FP32", "f16": "FP16 deviation-form", "bf16": "BF16 deviation-form"}
 
 
 def g_storage(cfg, variant: int = -1) -> str:
@@ -188,7 +192,7 @@ G_POPULATIONS = False
 VARIANT, ZCHUNK = -1, 0
 
 
-def make_solver(storage: str, device: int):
+def make_solver(storage: str, device: int, tau_g: float | None = None):
     import mcb
 
     cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=SCALE)
@@ -196,6 +200,8 @@ def make_solver(storage: str, device: int):
     cfg.device = device
     if G_POPULATIONS:
         cfg.g_mode = mcb.G_POPULATIONS
+    if tau_g is not None:
+        cfg.tau_g = tau_g
     cfg.variant, cfg.zchunk = VARIANT, ZCHUNK
     s = mcb.Solver(cfg)
     return s, cfg, (phi, ux, uy, uz)
@@ -210,9 +216,9 @@ def pinned_like(a):
     return t, v
 
 
-def device_run(storage, device, steps, warmup, dist):
+def device_run(storage, device, steps, warmup, dist, tau_g=None):
     """Device-resident timing: K updates, an event after every kernel."""
-    s, cfg, fields = make_solver(storage, device)
+    s, cfg, fields = make_solver(storage, device, tau_g)
     s.set_fields(*fields)
     s.step(warmup)
     s.synchronize()
@@ -255,6 +261,7 @@ def e2e_run(device, steps, save=100):
     return {"value": cells * steps / (t1 - t0) / 1e6, "unit": "MLUPS",
             "h2d_bytes_per_step": 4 * 4 * cells / steps,
             "d2h_bytes_per_step": 4 * cells * reads / steps,
+            "steps": steps,
             "note": f"H2D of phi,u from pinned host once; D2H of phi every {save} updates"}
 
 
@@ -277,6 +284,131 @@ def reference_cuda_run(device, steps):
     return {"value": nx * ny * nz * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
             "config": "128x128x256 frozen-shell mode, one stream, 10 launches per update",
             "steps": steps}
+
+
+def storage_leg(device, steps, warmup, storage, tau_g=None):
+    """One device leg of the bench workload: MLUPS and the collide kernel's roofline at the
+    given storage (and g relaxation time)."""
+    cfg, total, t_phi, t_col, d = device_run(storage, device, steps, warmup, None, tau_g)
+    cells = cfg.nx * cfg.ny * cfg.nz
+    hbm, peak_kind = peaks()
+    _, col_b, upd_b = bytes_per_lu(cfg, storage)
+    col_s = t_col * 1e-3 / steps
+    return {"storage": storage, "tau_g": cfg.tau_g, "g_storage": g_storage(cfg),
+            "value": cells * steps / (total * 1e-3) / 1e6, "unit": "MLUPS", "steps": steps,
+            "kernel_ms": {"phi_stage": t_phi / steps, "k_collide": t_col / steps},
+            "roofline": {"bytes_per_lu": col_b, "achieved": col_b * cells / col_s / 1e9,
+                         "peak": hbm, "unit": "GB/s",
+                         "frac": col_b * cells / col_s / 1e9 / hbm,
+                         "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                         "update_bytes_per_lu": upd_b},
+            "finite": bool(d["finite"])}
+
+
+def reference_mode_run(device, steps, nx=128, ny=128, nz=256, tau=0.7, sigma=0.05, r=16.0,
+                       width=4.0, sharp_c=None):
+    """The solver in the reference's frozen-shell mode (MCB_BC_REF) on the reference
+    kernels' own setting: one centred bubble (initPhase's formula), tau_g = 1."""
+    import mcb
+
+    cfg = mcb.default_config(nx=nx, ny=ny, nz=nz, bc=mcb.BC_REF, tau=tau, tau_g=1.0,
+                             sigma=sigma, width=width, device=device,
+                             sharp_c=sharp_c if sharp_c is not None else 0.0)
+    phi = mcb.fill_phi_reference(nx, ny, nz, r, width)
+    cells = nx * ny * nz
+    with mcb.Solver(cfg) as s:
+        s.set_fields(phi)
+        s.step(34)
+        total, _, t_col = s.step_profiled(steps)
+    return {"value": cells * steps / (total * 1e-3) / 1e6, "unit": "MLUPS", "steps": steps,
+            "config": f"{nx}x{ny}x{nz} frozen-shell mode, tau {tau}, sigma {sigma}, "
+                      f"R {r}, W {width}, FP32",
+            "k_collide_ms": t_col / steps}
+
+
+def reference_cuda_stock(device, steps):
+    """The reference's own kernels at the reference's stock setting: 64x64x256, tau 0.505,
+    sigma 0.1, SHARP_C 0.45 (src/var.cu:3-25), R 20 and width 3 (src/init.cu:39,46)."""
+    from oracle.oracle import ReferenceKernels, harness_available
+    import mcb
+
+    if not harness_available():
+        return {"unavailable": "reference cubin not present"}
+    nx, ny, nz = 64, 64, 256
+    phi = mcb.fill_phi_reference(nx, ny, nz, 20.0, 3.0)
+    rk = ReferenceKernels(nx, ny, nz, 0.505, 0.1, 0.45, device=device)
+    rk.set_phi(phi)
+    rk.run(5)
+    ms = rk.run(steps)
+    rk.close()
+    return {"value": nx * ny * nz * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
+            "config": "64x64x256 stock constants, one stream, 10 launches per update",
+            "steps": steps}
+
+
+CONFIG3_UPDATES = 5000
+
+
+def config3_run(device, updates=CONFIG3_UPDATES):
+    """The precision study as configured: 256^3 periodic, 32 bubbles R ~ U[6, 16], velocity
+    noise 1e-4, tau 0.6, sigma 0.05, W 4, run for the full number of updates with FP32,
+    FP16 and BF16 population storage. Reports device MLUPS and the exact phi-mass drift of
+    each, and how far the 16-bit runs end from the FP32 run. The errors against the FP64
+    oracle come from the 64^3 crop rerun in the GPU tests."""
+    import mcb
+
+    cfg, phi, ux, uy, uz = mcb.workload(3, seed=SEED)
+    cfg.device = device
+    cells = cfg.nx * cfg.ny * cfg.nz
+    out, last = {}, {}
+    for st in ("f32", "f16", "bf16"):
+        cfg.storage = mcb.STORAGES[st]
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, ux, uy, uz)
+            s.step(1)
+            m0 = s.diagnostics()["mass_q30"]
+            s.step(updates - 1)
+            ms = s.last_step_ms()
+            d = s.diagnostics(allow_nonfinite=True)
+            last[st] = {k: s.get(k) for k in ("phi", "ux", "uy", "uz")}
+        out[st] = {"mlups": cells * (updates - 1) / (ms * 1e-3) / 1e6,
+                   "mass_drift_q30": int(d["mass_q30"] - m0), "finite": bool(d["finite"]),
+                   "kinetic": d["kinetic"]}
+    for st in ("f16", "bf16"):
+        out[st]["max_phi_diff_vs_f32"] = float(np.max(np.abs(last[st]["phi"] - last["f32"]["phi"])))
+        out[st]["max_u_diff_vs_f32"] = float(max(np.max(np.abs(last[st][k] - last["f32"][k]))
+                                                 for k in ("ux", "uy", "uz")))
+    out["cells"] = cells
+    out["updates"] = updates
+    out["ratio_f16_vs_f32"] = out["f16"]["mlups"] / out["f32"]["mlups"]
+    out["ratio_bf16_vs_f32"] = out["bf16"]["mlups"] / out["f32"]["mlups"]
+    return out
+
+
+def laplace_run(device, updates=2000):
+    """The static bubble (64^3 periodic, R 12, W 4, tau 0.8, sigma 0.1, tau_g 0.8): the
+    Laplace-law error dp R / (2 sigma) - 1 after the full run, per storage, with R the radius
+    of the phi > 1/2 volume. The lattice fits in L2, so its MLUPS are not a roofline figure."""
+    import math
+
+    import mcb
+
+    cfg, phi, ux, uy, uz = mcb.workload(1, seed=SEED)
+    cfg.device = device
+    cells = cfg.nx * cfg.ny * cfg.nz
+    out = {}
+    for st in ("f32", "f16", "bf16"):
+        cfg.storage = mcb.STORAGES[st]
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, ux, uy, uz)
+            s.step(updates)
+            ms = s.last_step_ms()
+            d = s.diagnostics()
+        r = (3 * d["vol_half"] / (4 * math.pi)) ** (1 / 3)
+        out[st] = {"laplace_err": d["dp"] * r / (2 * cfg.sigma) - 1, "dp": d["dp"],
+                   "R_half": r, "mlups": cells * updates / (ms * 1e-3) / 1e6}
+    out["updates"] = updates
+    return out
 
 
 def batch_run(device, steps, ncases=64):
@@ -355,12 +487,13 @@ def swarm_run(device, steps):
 
 
 def cpu_baseline(seconds=10.0, threads=None):
-    """FP64 oracle on the host cores: the scenario at half scale (64x64x128)."""
+    """FP64 oracle on the host cores: the bench workload at full size, as many updates as
+    fit in the given seconds."""
     import mcb
-    from oracle.oracle import Oracle, threads_available
+    from oracle.oracle import Oracle
 
     threads = threads or os.cpu_count() or 1
-    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=0.5)
+    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=SCALE)
     o = Oracle.from_config(cfg, threads=threads)
     o.set_fields(phi, ux, uy, uz)
     o.step(1)
@@ -371,7 +504,7 @@ def cpu_baseline(seconds=10.0, threads=None):
     dt = time.perf_counter() - t0
     cells = cfg.nx * cfg.ny * cfg.nz
     return {"value": cells * n / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
-            "sample": f"FP64 oracle, the same scenario at half scale ({cfg.nx}x{cfg.ny}x{cfg.nz}),"
+            "sample": f"FP64 oracle, the bench workload ({cfg.nx}x{cfg.ny}x{cfg.nz}),"
                       f" {n} updates in {dt:.1f} s"}
 
 
@@ -389,31 +522,39 @@ def traffic_per_launch(cells, storage="f32", gs="push"):
 
 
 def run_reference_arm(args, ws, rank):
+    """The reference path on the host cores: the FP64 oracle port of the reference update
+    (the reference has no CPU implementation) on the full 128x128x256 rising bubble. The
+    initial field comes from the oracle-side generator, so this arm loads no solver code."""
     if rank != 0:
         return
     steps, warmup = args.steps, args.warmup
-    import mcb
     from oracle.oracle import Oracle
+    from oracle.workload_port import rising_bubble
 
     threads = os.cpu_count() or 1
-    cfg, phi, ux, uy, uz = mcb.workload(SCENARIO, seed=SEED, scale=0.5)
-    o = Oracle.from_config(cfg, threads=threads)
-    o.set_fields(phi, ux, uy, uz)
+    phi, p = rising_bubble(seed=SEED, scale=SCALE)
+    f32 = lambda v: float(np.float32(v))
+    sharp = (p["tau_g"] - 0.5) * 4.0 / p["width"]
+    o = Oracle(p["nx"], p["ny"], p["nz"], p["bc"], f32(p["tau"]), f32(p["tau_g"]),
+               f32(p["sigma"]), f32(sharp), f32(p["gravity"]), threads=threads)
+    o.set_fields(phi)
     o.step(warmup)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
-    cells = cfg.nx * cfg.ny * cfg.nz
+    cells = p["nx"] * p["ny"] * p["nz"]
     v = cells * steps / dt / 1e6
-    sample = (f"FP64 oracle port of the reference update (the reference has no CPU path), "
-              f"scenario at half scale {cfg.nx}x{cfg.ny}x{cfg.nz}, {steps} updates")
+    sample = (f"FP64 oracle port of the reference update (the reference has no CPU path) on "
+              f"the full {p['nx']}x{p['ny']}x{p['nz']} rising bubble, {steps} updates after "
+              f"{warmup} warm-up updates, {threads} threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": ws,
         "steps": steps, "warmup": warmup, "ms_per_step": dt * 1e3 / max(steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "rising perturbed bubble, walls z, gravity 1e-5 (half scale "
-                               "sample)", "cells": cells},
+        "config": {"workload": f"rising perturbed bubble {p['nx']}x{p['ny']}x{p['nz']}, walls "
+                               "z, gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4",
+                   "cells": cells, "same_config": True, "seed": SEED},
         "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -489,10 +630,11 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "storage": st,
         "data": "synthetic",
         "config": {"workload": f"rising perturbed bubble {cfg.nx}x{cfg.ny}x{cfg.nz}, walls z, "
-                               "gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, FP32 "
-                               "storage",
+                               "gravity 1e-5, Y_lm l=2..6, tau 0.7, sigma 0.05, W 4, "
+                               f"{STORAGE_WORDS[st]} population storage",
                    "cells": cells,
-                   "l2": "inputs larger than L2 (f in and out: 638 MB per update, FP32)",
+                   "l2": f"inputs larger than L2 (f in and out: "
+                         f"{2 * 19 * (4 if st == 'f32' else 2) * cells / 1e6:.0f} MB per update)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
         "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
@@ -512,18 +654,35 @@ def main():
     if rank == 0 and args.only_device:
         print(json.dumps(result))
     elif rank == 0:
-        _, t16, p16, c16, d16 = device_run("f16", local, args.steps, args.warmup, None)
-        v16 = cells * args.steps / (t16 * 1e-3) / 1e6
-        result["fp16"] = {"value": v16, "unit": "MLUPS", "ratio_vs_f32": v16 / (value / ws),
-                          "frac_update": bytes_per_lu(cfg, "f16", VARIANT)[2] * cells
-                          / (t16 * 1e-3 / args.steps) / 1e9 / hbm,
-                          "kernel_ms": {"phi_stage": p16 / args.steps, "k_collide": c16 / args.steps}}
+        legs = {k: storage_leg(local, args.steps, args.warmup, k) for k in ("f16", "bf16")}
+        v32 = value / ws
+        for k, leg in legs.items():
+            leg["ratio_vs_f32"] = leg["value"] / v32
+        result["fp16"], result["bf16"] = legs["f16"], legs["bf16"]
+        # stored, relaxed g (tau_g = 0.8, the static-bubble setting) on the same workload
+        result["stored_g"] = [storage_leg(local, args.steps, args.warmup, k, tau_g=0.8)
+                              for k in ("f32", "f16")]
         result["e2e"] = e2e_run(local, args.steps)
+        result["e2e_500"] = e2e_run(local, 500)
         if not args.no_extras:
+            result["config3"] = config3_run(local)
+            result["laplace"] = laplace_run(local)
             result["batch"] = batch_run(local, min(args.steps, 200))
             result["swarm"] = swarm_run(local, min(args.steps, 50))
             result["d3q27"] = [d3q27_run(local, min(args.steps, 200), st) for st in ("f32", "f16")]
-        result["reference_cuda"] = reference_cuda_run(local, min(args.steps, 200))
+        nref = min(max(args.steps, 20), 200)
+        rc = reference_cuda_run(local, nref)
+        mine = reference_mode_run(local, nref)
+        if "value" in rc:
+            mine["ratio_vs_reference_cuda"] = mine["value"] / rc["value"]
+        result["reference_cuda"] = rc
+        result["reference_mode"] = mine
+        stock = reference_cuda_stock(local, nref)
+        mine_stock = reference_mode_run(local, nref, 64, 64, 256, 0.505, 0.1, 20.0, 3.0, 0.45)
+        if "value" in stock:
+            mine_stock["ratio_vs_reference_cuda"] = mine_stock["value"] / stock["value"]
+        result["reference_cuda_stock"] = stock
+        result["reference_mode_stock"] = mine_stock
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         print(json.dumps(result))
     barrier(dist)

@@ -164,6 +164,11 @@ int  mcb_synchronize(mcb_handle* h);
  * MCB_BC_REF the shell of phi holds the zero-gradient copy, as in the reference's dumps. */
 int  mcb_get_field(mcb_handle* h, int which, float* host);
 
+/* Copies the exact Q2.30 phi of the latest update (1.0 = 2^30) to a host array of nx*ny*nz
+ * int32, x fastest. These are the integers whose sum (over the interior for MCB_BC_REF) is
+ * mcb_diag.mass_q30. No counterpart in the reference, which keeps phi in float32. */
+int  mcb_get_phi_q30(mcb_handle* h, int32_t* host);
+
 /* FP64 reductions over the latest update (replaces the placeholders of
  * src/auxFunctions.cu:24-40). Returns MCB_ERR_NUMERIC, with out filled, if a value is
  * not finite. */
@@ -247,16 +252,23 @@ int  mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk
  * No counterpart in the reference. It exists for callers that cannot call cudaMalloc:
  *   - a host code that owns all device memory through its own pool, sized at start-up;
  *   - a loop that must not risk the device-wide synchronisation cudaFree can imply.
- * It computes what mcb_diagnostics computes, from:
+ * It computes the reductions of mcb_diagnostics from:
  *   - phi, rho, ux, uy, uz: device arrays of nx*ny*nz floats, x fastest;
- *   - phi_q30: the matching Q2.30 phi, or NULL to take the integer mass from phi.
+ *   - phi_q30: the matching Q2.30 phi (mcb_get_phi_q30 gives a handle's), or NULL to take
+ *     the integer mass from phi rounded to Q2.30.
+ * kinetic is 0.5 * rho * |u|^2 with rho the given rho field. That is what mcb_diagnostics
+ * computes for density-matched cases. With a density ratio (rho_in != rho_out) a handle's
+ * rho field holds p / cs^2, and mcb_diagnostics takes the density rho_out + (rho_in -
+ * rho_out) phi instead, so the two kinetic energies differ there; every other value agrees.
  * It enqueues the reduction on `stream` (NULL: the default stream) and waits for the
  * result. bc = MCB_BC_REF leaves the shell out, as mcb_diagnostics does.
  * It allocates nothing on the device or the host. Its scratch is one file-scope device
  * array of 305 records (about 29 KB), fixed whatever the lattice size, and every GPU that
  * loads the library holds it until exit.
- * The first call on a device looks up that array's device address. Make that first call
- * before any stream capture on the device.
+ * Every call looks up that array's device address in the current context with
+ * cudaGetSymbolAddress (not a stream operation), so a context reset between calls is
+ * harmless. The first call on a device may load the library's kernels into its context:
+ * make that first call before any stream capture on the device.
  * All calls share the array. Calls that overlap on the GPU (other host threads, other
  * streams) race and must be serialised by the caller. No scratch needs clearing: every
  * block overwrites its own record. Lattices above MCB_DIAG_DEVICE_MAX_CELLS cells are

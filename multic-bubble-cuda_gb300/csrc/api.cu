@@ -123,6 +123,8 @@ struct Solver {
   int ratio = 0;           // density-ratio model
   int wide = 0;            // some case needs 64-bit f offsets
   bool padded = false;     // f in the padded layout of the TMA collide
+  bool pair_ok = false;    // the two-cells-per-thread kernel can run these cases
+  bool wide_blocked = false;  // 64-bit f offsets on the blocked layout: the pair kernel only
   bool push = false;       // the collide kernel writes the next phi (all but the TMA kernel)
   CUtensorMap fmap[2];     // TMA descriptors of f[0], f[1] (padded only)
   int* err = nullptr;      // device error flag of bounded waits
@@ -357,10 +359,18 @@ struct Solver {
       max_blocked = std::max(max_blocked, ((d.nx + 31) / 32) * 32LL * d.ny * d.nz);
     const char* force_wide = std::getenv("MCB_WIDE_OFFSETS");
     wide = max_blocked * qf >= (1LL << 31) || (force_wide && force_wide[0] == '1');
+    // The two-cells-per-thread kernel: equilibrium g, D3Q19 f at density ratio 1, an even nx
+    // in every case. It addresses f per plane with 64-bit plane offsets, so it also runs the
+    // cases that need 64-bit f offsets, on the blocked layout.
+    pair_ok = gmode == mcb::kGEquil && qf == 19 && !ratio && !padded;
+    for (auto& d : cases) pair_ok = pair_ok && d.nx % 2 == 0;
+    if (variant == mcb::kPairVariant && !pair_ok) variant = 0;
     // f layout: blocked with equilibrium g and 32-bit offsets (x rounded up to whole 32-cell
-    // blocks); plain otherwise (the 64-bit kernels and the stored-g ones measured slower
-    // blocked: they spill the extra per-thread offsets). The padded TMA layout is set below.
-    const bool blocked = gmode == mcb::kGEquil && !wide;
+    // blocks), or with the pair kernel at any size; plain otherwise (the 64-bit one-cell
+    // kernels and the stored-g ones measured slower blocked: they spill the extra per-thread
+    // offsets). The padded TMA layout is set below.
+    const bool blocked = gmode == mcb::kGEquil && (!wide || variant == mcb::kPairVariant);
+    wide_blocked = wide && blocked;
     f_cells_total = max_f_cells = 0;
     for (auto& d : cases) {
       d.fxb = blocked ? (d.nx + 31) / 32 : 0;
@@ -371,7 +381,8 @@ struct Solver {
     }
     if (wide) padded = false;
     if (padded) variant = mcb::kTmaVariant;
-    else if (variant == mcb::kTmaVariant || qf == 27 || ratio || wide) variant = 0;
+    else if (variant == mcb::kTmaVariant || qf == 27 || ratio || (wide && !wide_blocked))
+      variant = 0;
     for (auto& d : cases) {
       if (padded) {
         d.fgx = gxe;
@@ -729,6 +740,12 @@ struct Solver {
     return v;
   }
 
+  // f layout of the checkpoint header: the ghost width of the padded layout, -1 blocked,
+  // 0 plain.
+  int layout_code() const {
+    return padded ? cases[0].fgx : (cases[0].fxb > 0 ? -1 : 0);
+  }
+
   int ckpt_save(const char* path) {
     if (!path) return fail(MCB_ERR_INVALID, "path is NULL");
     if (cases.size() != 1) return fail(MCB_ERR_INVALID, "checkpoints hold one case");
@@ -749,7 +766,7 @@ struct Solver {
     hd.first = first;
     hd.latest_p = latest_p;
     hd.pk = pk;
-    hd.pad = padded ? cases[0].fgx : 0;  // f layout
+    hd.pad = layout_code();  // f layout
     hd.qf = qf;
     hd.ratio = ratio;
     hd.update = update;
@@ -792,7 +809,7 @@ struct Solver {
     }
     mcb::CaseDesc& d = cases[0];
     if (hd.nx != d.nx || hd.ny != d.ny || hd.nz != d.nz || hd.bc != d.bc ||
-        hd.storage != storage || hd.gmode != gmode || hd.pad != (padded ? d.fgx : 0) ||
+        hd.storage != storage || hd.gmode != gmode || hd.pad != layout_code() ||
         hd.qf != qf || hd.ratio != ratio) {
       std::fclose(fp);
       return fail(MCB_ERR_INVALID,
@@ -872,6 +889,21 @@ struct Solver {
           }
     }
     return MCB_OK;
+  }
+
+  // The exact Q2.30 phi of the latest update (the integers the diagnostics sum).
+  int get_phi_q30(int ci, int32_t* host) {
+    if (ci < 0 || ci >= static_cast<int>(cases.size()))
+      return fail(MCB_ERR_INVALID, "case index %d out of range", ci);
+    if (!host) return fail(MCB_ERR_INVALID, "host pointer is NULL");
+    if (!fields_set[ci]) return fail(MCB_ERR_STATE, "fields of case %d are not set", ci);
+    MCB_TRY(set_device());
+    const mcb::CaseDesc& d = cases[ci];
+    MCB_CU(cudaMemcpyAsync(host, p[latest_p] + d.cell_off,
+                           static_cast<size_t>(d.ncell) * sizeof(int32_t),
+                           cudaMemcpyDeviceToHost, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    return check_err();
   }
 
   int diagnostics(int ci, mcb_diag* out) {
@@ -1009,6 +1041,11 @@ int mcb_synchronize(mcb_handle* h) {
 int mcb_get_field(mcb_handle* h, int which, float* host) {
   if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
   return h->s.get_field(0, which, host);
+}
+
+int mcb_get_phi_q30(mcb_handle* h, int32_t* host) {
+  if (!h) return fail(MCB_ERR_INVALID, "handle is NULL");
+  return h->s.get_phi_q30(0, host);
 }
 
 int mcb_diagnostics(mcb_handle* h, mcb_diag* out) {
@@ -1223,6 +1260,8 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
     // plain tiles otherwise.
     if ((v == mcb::kTmaVariant) != s.padded) continue;
     if ((s.qf == 27 || s.ratio) && v != 0) continue;  // these run the 32x8 tile
+    if (v == mcb::kPairVariant && !s.pair_ok) continue;
+    if (s.wide_blocked && v != mcb::kPairVariant) continue;
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;
       s.variant = v;

@@ -2,7 +2,6 @@
 #include <cfloat>
 #include <cstdint>
 #include <cstdio>
-#include <mutex>
 
 #include "mcb.h"
 #include "solver.h"
@@ -284,9 +283,6 @@ static __device__ __align__(256) mcb::DiagPartial g_diag_scratch[mcb::kDiagBlock
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-mcb::DiagPartial* g_scratch_addr[kMaxDevices] = {};
 thread_local char g_dev_err[256];
 
 int dev_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
@@ -296,23 +292,17 @@ int dev_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
   return code;
 }
 
-// Device address of the scratch array on the current device. In host code the array's name
-// is only a host-side stand-in, so the address comes from cudaGetSymbolAddress, once per
-// device, on the first call made with that device current.
-int scratch_on_current_device(mcb::DiagPartial** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return dev_fail(MCB_ERR_CUDA, "cudaGetDevice failed", e);
-  if (dev < 0 || dev >= kMaxDevices) return dev_fail(MCB_ERR_INVALID, "device ordinal >= 64");
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_diag_scratch);
-    if (e != cudaSuccess || !p)
-      return dev_fail(MCB_ERR_CUDA, "cudaGetSymbolAddress of the diagnostics scratch failed", e);
-    g_scratch_addr[dev] = static_cast<mcb::DiagPartial*>(p);
-  }
-  *out = g_scratch_addr[dev];
+// Device address of the scratch array in the current context. In host code the array's name
+// is only a host-side stand-in, so the address comes from cudaGetSymbolAddress. It is looked
+// up on every call, not cached: it is not a stream operation, it costs far less than the
+// reduction, and a context torn down and created again (cudaDeviceReset, for one) may load the
+// module at another address, which a cached pointer would miss.
+int scratch_in_current_context(mcb::DiagPartial** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_diag_scratch);
+  if (e != cudaSuccess || !p)
+    return dev_fail(MCB_ERR_CUDA, "cudaGetSymbolAddress of the diagnostics scratch failed", e);
+  *out = static_cast<mcb::DiagPartial*>(p);
   return MCB_OK;
 }
 
@@ -332,7 +322,7 @@ extern "C" int mcb_diagnostics_device(const float* phi, const float* rho, const 
   if (bc != MCB_BC_REF && bc != MCB_BC_PERIODIC && bc != MCB_BC_WALLS_Z)
     return dev_fail(MCB_ERR_INVALID, "mcb_diagnostics_device: unknown boundary mode");
   mcb::DiagPartial* scratch = nullptr;
-  const int rc = scratch_on_current_device(&scratch);
+  const int rc = scratch_in_current_context(&scratch);
   if (rc != MCB_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   mcb::k_diag_fields<<<mcb::kDiagBlocks, mcb::kDiagThreads, 0, s>>>(

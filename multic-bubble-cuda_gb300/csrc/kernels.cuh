@@ -1432,6 +1432,14 @@ __global__ void k_init(const InitArgs a) {
   });
 }
 
+}  // namespace
+}  // namespace mcb
+
+#include "kernels_pair.cuh"
+
+namespace mcb {
+namespace {
+
 // ------------------------------------------------------------------------ dispatch --
 
 // Kernel entry and block shape of each tile variant (kVariants order).
@@ -1445,6 +1453,7 @@ template <class S>
 const void* phi_kernel(int variant, bool eq, dim3* block) {
   switch (variant) {
     case 0:
+    case kPairVariant:
     case kTmaVariant: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
     case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
     case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
@@ -1460,6 +1469,14 @@ const void* collide_kernel(int variant, dim3* block) {
     case 1: *block = dim3(16, 16); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 16>);
     case 2: *block = dim3(64, 4); return reinterpret_cast<const void*>(k_collide<S, GM, 64, 4>);
     case 3: *block = dim3(16, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 8>);
+    case kPairVariant:
+      // two cells per thread: equilibrium g only
+      if constexpr (GM == kGEquil) {
+        *block = dim3(kPairTX, kPairBY);
+        return reinterpret_cast<const void*>(k_collide_pair<S, kPairBY>);
+      } else {
+        return nullptr;
+      }
     default: return nullptr;
   }
 }
@@ -1529,7 +1546,7 @@ cudaError_t prepare_tma_kernel() {
 template <class S>
 cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int wide, int* phi_blocks,
                          int* collide_blocks) {
-  if (qf == kQ27 || ratio || wide) {
+  if (variant != kPairVariant && (qf == kQ27 || ratio || wide)) {
     dim3 bp;
     const void* fp = phi_kernel<S>(0, gmode == kGEquil, &bp);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -1580,7 +1597,7 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
                                       const void* tmap, cudaStream_t s) {                  \
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
-    if (a.qf == kQ27 || a.ratio || a.wide)                                                 \
+    if (variant != kPairVariant && (a.qf == kQ27 || a.ratio || a.wide))                    \
       return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0, a.wide != 0),        \
                        a.grid_collide, dim3(32, 8), a, s);                                 \
     dim3 block;                                                                            \

@@ -1,0 +1,545 @@
+// k_collide_pair: the equilibrium-g update of k_collide with two neighbouring cells in x per
+// thread, for D3Q19 f at density ratio 1 (the reference's model) on the blocked f layout.
+//
+// It computes what k_collide computes (gradCalc, curvatureCalc, momentiCalc, collisionFluid,
+// collisionPhase, streamingCalc and phiCalc of src/lbm.cu, fgBoundary and
+// boundaryConditions in reference mode), in the same order per cell. What changes is the
+// shape of the work:
+//   - a thread owns cells x0 = xt + 2 tx and x0 + 1 of one row, so every arithmetic step of
+//     the moments, the curvature, the force and the collisions runs once for both cells in
+//     packed FP32 (FFMA2, FADD2, FMUL2: each lane the IEEE single-precision operation);
+//   - the populations that do not move in x (9 of 19) are gathered for both cells with one
+//     aligned 64-bit (FP32) or 32-bit (16-bit storage) load, and all 19 post-collision
+//     populations are stored for both cells with one such store each; 16-bit storage packs
+//     the pair with one conversion;
+//   - the 19 integer g populations of the two cells are summed per target before the shared
+//     atomics where their targets coincide (28 atomics for the pair instead of 38);
+//   - the per-plane and per-segment work (phi ring, offsets, loop) is shared by two cells.
+// Arithmetic and the exact integer push of phi are those of k_collide, so results agree with
+// it to FP32 rounding (the fused multiply-adds are placed explicitly here). Requires an even
+// nx in every case, so that a pair never straddles the lattice edge.
+#pragma once
+
+namespace pk {
+
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+// a - b, exactly rounded: b * (-1) is exact, so the fused operation rounds once.
+__device__ __forceinline__ float2 sub(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+__device__ __forceinline__ float2 scale(float2 a, float c) { return __fmul2_rn(a, dup(c)); }
+// s * a + b for a compile-time sign s = +1 or -1.
+template <int Sg>
+__device__ __forceinline__ float2 addsg(float2 b, float2 a) {
+  if constexpr (Sg > 0) return add(b, a);
+  else return sub(b, a);
+}
+
+// Pair loads and stores of the storage formats. Deviation storage (16-bit) returns the
+// stored f - W; the moments add the weights' moments.
+template <class S>
+struct PairIO;
+template <>
+struct PairIO<mcb::StF32> {
+  using FT = float;
+  static __device__ __forceinline__ float2 ld2(const float* p) {
+    return __ldg(reinterpret_cast<const float2*>(p));
+  }
+  static __device__ __forceinline__ float ld1(const float* p) { return __ldg(p); }
+  static __device__ __forceinline__ void st2(float* p, float2 v) {
+    *reinterpret_cast<float2*>(p) = v;
+  }
+};
+template <>
+struct PairIO<mcb::StH16> {
+  using FT = __half;
+  static __device__ __forceinline__ float2 ld2(const __half* p) {
+    return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+  }
+  static __device__ __forceinline__ float ld1(const __half* p) { return __half2float(__ldg(p)); }
+  static __device__ __forceinline__ void st2(__half* p, float2 v) {
+    *reinterpret_cast<__half2*>(p) = __float22half2_rn(v);
+  }
+};
+template <>
+struct PairIO<mcb::StB16> {
+  using FT = __nv_bfloat16;
+  static __device__ __forceinline__ float2 ld2(const __nv_bfloat16* p) {
+    return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)));
+  }
+  static __device__ __forceinline__ float ld1(const __nv_bfloat16* p) {
+    return __bfloat162float(__ldg(p));
+  }
+  static __device__ __forceinline__ void st2(__nv_bfloat16* p, float2 v) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __float22bfloat162_rn(v);
+  }
+};
+
+}  // namespace pk
+
+namespace mcb {
+namespace {
+
+constexpr int kPairTX = 32;  // threads in x; a tile is 2 * kPairTX = 64 cells wide
+
+template <class S, int BY>
+__device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Tile& t) {
+  using FT = typename S::FT;
+  using IO = pk::PairIO<S>;
+  using pk::add;
+  using pk::dup;
+  using pk::fma;
+  using pk::mul;
+  using pk::scale;
+  using pk::sub;
+  constexpr int TX = kPairTX, BX = 2 * TX, NT = TX * BY;
+  constexpr int PX = BX + 4, PY = BY + 4, PP = PX * PY;  // phi plane, halo 2
+  constexpr int PH = PX / 2, PP2 = PP / 2;              // the same in pairs of values
+  constexpr int KP2 = (PP2 + NT - 1) / NT;              // phi pairs per thread per plane
+  constexpr int HX = BX + 2, HY = BY + 2, HP = HX * HY;  // normals plane, halo 1
+  constexpr int KFL = (HP + NT - 1) / NT;                // ring positions per thread
+  constexpr bool kDevF = S::kFDev;
+  constexpr int QF = kQ;
+  __shared__ __align__(16) float sphi[5][PP];
+  __shared__ __align__(16) float snrm[4][4][HP];  // nx, ny, nz, |grad phi| of four planes
+  __shared__ __align__(16) int sacc[4][HP];       // push ring: integer sums of the next phi
+  __shared__ int scen[HP];
+
+  const int nx = t.nx, ny = t.ny, nz = t.nz;
+  const int nxy = nx * ny;
+  const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
+  const int x0 = t.xt + 2 * tx, y = t.yt + ty;
+  const bool active = x0 < nx && y < ny;  // nx is even: x0 + 1 < nx with x0
+
+  const CaseDesc* cd = a.cases + t.ci;
+  const float omega = __ldg(&cd->omega);
+  const float sigma = __ldg(&cd->sigma), sharp_c = __ldg(&cd->sharp_c);
+  const float gravity = __ldg(&cd->gravity), phi_mean = __ldg(&cd->phi_mean);
+
+  const int* __restrict__ pcur = a.p_cur + t.cell_off;
+  int* __restrict__ pnext = a.p_next + t.cell_off;
+  int* __restrict__ pzero = a.p_zero + t.cell_off;
+
+  // Halo pairs of a phi plane handled by this thread (in-plane offsets, even: the pair is
+  // one aligned 64-bit load). Periodic axes wrap; in reference mode x clamps to the lattice
+  // (the values beyond the shell only feed normals that are zero there).
+  int hoff[KP2];
+#pragma unroll
+  for (int k = 0; k < KP2; ++k) {
+    const int i = tid + k * NT;
+    hoff[k] = 0;
+    if (i < PP2) {
+      int gx = t.xt - 2 + 2 * (i % PH), gy = t.yt - 2 + i / PH;
+      if (ref) {
+        gx = clampi(gx, 0, nx - 2);
+        gy = clampi(gy, 0, ny - 1);
+      } else {
+        gx = ((gx % nx) + nx) % nx;
+        gy = ((gy % ny) + ny) % ny;
+      }
+      hoff[k] = gx + gy * nx;
+    }
+  }
+  auto zmap = [&](int z) -> int {
+    if (t.bc == kBcPeriodic) z = wrap1(z, nz);
+    else if (walls) z = z < 0 ? -1 - z : (z >= nz ? 2 * nz - 1 - z : z);  // mirror
+    return clampi(z, 0, nz - 1);
+  };
+  int2 pre[KP2];
+  auto issue = [&](int zpl) {
+    const int* base = pcur + static_cast<long long>(zmap(zpl)) * nxy;
+#pragma unroll
+    for (int k = 0; k < KP2; ++k)
+      if (tid + k * NT < PP2) pre[k] = __ldg(reinterpret_cast<const int2*>(base + hoff[k]));
+  };
+  auto commit = [&](int zpl) {
+    float2* d = reinterpret_cast<float2*>(sphi[(zpl + 5) % 5]);
+#pragma unroll
+    for (int k = 0; k < KP2; ++k)
+      if (tid + k * NT < PP2)
+        d[tid + k * NT] = scale(make_float2(__int2float_rn(pre[k].x), __int2float_rn(pre[k].y)),
+                                kInvQ30);
+  };
+
+  // Push ring: the global in-plane offsets of this thread's ring positions (-1: none).
+  int aoff[KFL];
+#pragma unroll
+  for (int k = 0; k < KFL; ++k) {
+    const int i = tid + k * NT;
+    aoff[k] = -1;
+    if (i >= HP) continue;
+    int gx = t.xt - 1 + i % HX, gy = t.yt - 1 + i / HX;
+    if (ref) {
+      if (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1) continue;
+    } else {
+      gx = ((gx % nx) + nx) % nx;
+      gy = ((gy % ny) + ny) % ny;
+    }
+    aoff[k] = gx + gy * nx;
+  }
+  for (int i = tid; i < 4 * HP; i += NT) (&sacc[0][0])[i] = 0;
+  auto flush = [&](int q) {
+    int* slot = sacc[(q + 8) % 4];
+    int qz = q;
+    if (t.bc == kBcPeriodic) qz = wrap1(q, nz);
+    const bool plane_ok = ref ? (qz > 0 && qz < nz - 1) : (qz >= 0 && qz < nz);
+#pragma unroll
+    for (int k = 0; k < KFL; ++k) {
+      const int i = tid + k * NT;
+      if (i >= HP) continue;
+      const int v = slot[i];
+      slot[i] = 0;
+      if (v != 0 && plane_ok && aoff[k] >= 0)
+        atomicAdd(pnext + aoff[k] + static_cast<long long>(qz) * nxy, v);
+    }
+  };
+
+  // Normals table: the phi-plane offset of normals point i, stored as -c - 1 where the
+  // normal is zero (reference-mode shell and beyond).
+  for (int i = tid; i < HP; i += NT) {
+    const int hx = i % HX, hy = i / HX;
+    const int gx = t.xt - 1 + hx, gy = t.yt - 1 + hy;
+    const bool zero = ref && (gx <= 0 || gx >= nx - 1 || gy <= 0 || gy >= ny - 1);
+    const int c = (hy + 1) * PX + hx + 1;
+    scen[i] = zero ? -c - 1 : c;
+  }
+  // Normals and |grad phi| of plane zp on the halo-1 region (gradCalc, src/lbm.cu:34-72), two
+  // points in x per thread in packed FP32, as k_collide computes them.
+  auto normals = [&](int zp) {
+    const float* pm = sphi[(zp + 4) % 5];
+    const float* p0 = sphi[(zp + 5) % 5];
+    const float* pp = sphi[(zp + 6) % 5];
+    float(*dst)[HP] = snrm[(zp + 4) % 4];
+    const bool zshell = ref && (zp <= 0 || zp >= nz - 1);
+    for (int j = tid; 2 * j < HP; j += NT) {
+      const int e0 = scen[2 * j], e1 = scen[2 * j + 1];
+      const int c = e0 >= 0 ? e0 : -e0 - 1;
+      float2 gx = dup(0.f), gy = gx, gz = gx;
+      static_for<1, kQ>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        constexpr float w3 = 3.0f * wf(L);
+        const float* q = nbr_of<cz(L)>(pm, p0, pp) + c + cy(L) * PX + cx(L);
+        const float2 v =
+            cx(L) != 0 ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
+        if constexpr (cx(L) != 0) gx = fma(dup(cx(L) * w3), v, gx);
+        if constexpr (cy(L) != 0) gy = fma(dup(cy(L) * w3), v, gy);
+        if constexpr (cz(L) != 0) gz = fma(dup(cz(L) * w3), v, gz);
+      });
+      const float2 g2 = fma(gz, gz, fma(gy, gy, mul(gx, gx)));
+      float2 fac = make_float2(rsqrtf(fmaxf(g2.x, 1e-9f)), rsqrtf(fmaxf(g2.y, 1e-9f)));
+      if (zshell || e0 < 0) fac.x = 0.f;
+      if (zshell || e1 < 0) fac.y = 0.f;
+      reinterpret_cast<float2*>(dst[0])[j] = mul(gx, fac);
+      reinterpret_cast<float2*>(dst[1])[j] = mul(gy, fac);
+      reinterpret_cast<float2*>(dst[2])[j] = mul(gz, fac);
+      reinterpret_cast<float2*>(dst[3])[j] = mul(g2, fac);
+    }
+  };
+
+  // Blocked f layout: population l of cell (x, y, z) at z*PS + y*RS + fx(x) + 32 l, with
+  // fx(x) = (x / 32) * 19 * 32 + x % 32. x0 is even, so x0 and x0 + 1 share a 32-cell block.
+  const FT* __restrict__ fin = static_cast<const FT*>(a.f_in) + t.f_off;
+  FT* __restrict__ fout = static_cast<FT*>(a.f_out) + t.f_off;
+  const int RS = t.fxb * (QF * 32);
+  const long long PS = static_cast<long long>(RS) * ny;
+  auto fxof = [](int xs) -> int { return (xs >> 5) * (QF * 32) + (xs & 31); };
+  const int xw = active ? x0 : 0;
+  const int fx0 = fxof(xw);                                     // x0 (and x0 + 1 at +1)
+  const int fxm = fxof(xw == 0 ? nx - 1 : xw - 1);              // x0 - 1
+  const int fxp = fxof(xw + 2 >= nx ? xw + 2 - nx : xw + 2);    // x0 + 2
+  const int yw = active ? y : 0;
+  const int fy0 = yw * RS;
+  const int fym = (yw == 0 ? ny - 1 : yw - 1) * RS;
+  const int fyp = (yw == ny - 1 ? 0 : yw + 1) * RS;
+  const int yo = yw * nx;
+
+  // Two cells' worth of one population: the gathered pair (values of x0, x0 + 1).
+  float2 fr[QF];
+
+  // Prologue: phi planes zb-2 .. zb+2, normals zb-1 .. zb+1.
+  for (int zpl = t.zb - 2; zpl <= t.zb + 2; ++zpl) {
+    issue(zpl);
+    commit(zpl);
+  }
+  issue(t.zb + 3);
+  __syncthreads();
+  for (int zpl = t.zb - 1; zpl <= t.zb + 1; ++zpl) normals(zpl);
+  __syncthreads();
+
+  for (int z = t.zb; z < t.ze; ++z) {
+    commit(z + 3);
+    if (z + 4 <= t.ze + 1) issue(z + 4);
+
+    const int idx = x0 + yo + z * nxy;
+    const bool zshell = ref && (z == 0 || z == nz - 1);
+    const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+    int2 pc = make_int2(0, 0);
+    if (active) {
+      pc = __ldg(reinterpret_cast<const int2*>(pcur + idx));
+      // Pull the 19 populations of both cells.
+      const FT* pz0 = fin + static_cast<long long>(z) * PS;
+      const FT* pzm = fin + static_cast<long long>(z == 0 ? nz - 1 : z - 1) * PS;
+      const FT* pzp = fin + static_cast<long long>(z == nz - 1 ? 0 : z + 1) * PS;
+      auto pull = [&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        const FT* row = src_of<cz(L)>(pzm, pz0, pzp) + src_of<cy(L)>(fym, fy0, fyp) + L * 32;
+        if constexpr (cx(L) == 0) {
+          fr[L] = IO::ld2(row + fx0);
+        } else if constexpr (cx(L) == 1) {  // sources x0 - 1 and x0
+          fr[L] = make_float2(IO::ld1(row + fxm), IO::ld1(row + fx0));
+        } else {  // sources x0 + 1 and x0 + 2
+          fr[L] = make_float2(IO::ld1(row + fx0 + 1), IO::ld1(row + fxp));
+        }
+      };
+      fr[0] = IO::ld2(pz0 + fy0 + fx0);
+      if (blo || bhi) {
+        // A wall plane: what left through the wall returns as the cell's own opposite
+        // population.
+        static_for<1, QF>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+          if (bounce) fr[L] = IO::ld2(pz0 + fy0 + fx0 + opp(L) * 32);
+          else pull(LC);
+        });
+      } else {
+        static_for<1, QF>(pull);
+      }
+    }
+    __syncthreads();
+    if (z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
+    if (z + 2 <= t.ze) normals(z + 2);
+    if (!active) continue;
+
+    *reinterpret_cast<int2*>(pzero + idx) = make_int2(0, 0);  // next update accumulates here
+    // Reference-mode shell cells of this pair (never collide; rest-equilibrium inflow).
+    const bool sh0 = ref && (zshell || x0 == 0 || y == 0 || y == ny - 1);
+    const bool sh1 = ref && (zshell || x0 + 1 == nx - 1 || y == 0 || y == ny - 1);
+
+    // Curvature (curvatureCalc, src/lbm.cu:80-125): kappa = -3 sum_l W_l c_l.n(x + c_l). The
+    // pair sits at normals offsets h0 (odd) and h0 + 1, so its x-1 and x+1 neighbours are
+    // aligned pairs; the x+0 neighbours are read as two values.
+    const float(*nm)[HP] = snrm[(z + 3) % 4];
+    const float(*n0)[HP] = snrm[(z + 4) % 4];
+    const float(*np)[HP] = snrm[(z + 5) % 4];
+    const int h0 = (ty + 1) * HX + 2 * tx + 1;
+    auto nrm2 = [&](const float(*pl)[HP], int comp, int o) -> float2 {
+      const float* q = &pl[comp][h0 + o];
+      return (o & 1) ? *reinterpret_cast<const float2*>(q) : make_float2(q[0], q[1]);
+    };
+    const float2 ncx = nrm2(n0, 0, 0), ncy = nrm2(n0, 1, 0), ncz = nrm2(n0, 2, 0);
+    const float2 ncw = nrm2(n0, 3, 0);
+    float2 kap = dup(0.f);
+    static_for<1, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      constexpr float w3 = 3.0f * wf(L);
+      const float(*pl)[HP] = nbr_of<cz(L)>(nm, n0, np);
+      constexpr int o = cy(L) * HX + cx(L);
+      float2 cn = dup(0.f);
+      if constexpr (cx(L) != 0) cn = pk::addsg<cx(L)>(cn, nrm2(pl, 0, o));
+      if constexpr (cy(L) != 0) cn = pk::addsg<cy(L)>(cn, nrm2(pl, 1, o));
+      if constexpr (cz(L) != 0) cn = pk::addsg<cz(L)>(cn, nrm2(pl, 2, o));
+      kap = fma(dup(-w3), cn, kap);
+    });
+    const float2 phi = *reinterpret_cast<const float2*>(&sphi[(z + 5) % 5][(ty + 2) * PX + 2 * tx + 2]);
+    const float2 mult = scale(kap, sigma);
+    const float2 mw = mul(mult, ncw);
+    float2 Fx = mul(mw, ncx), Fy = mul(mw, ncy), Fz = mul(mw, ncz);
+    if (gravity != 0.f) Fz = fma(dup(gravity), sub(phi, dup(phi_mean)), Fz);
+
+    // Moments (momentiCalc, src/lbm.cu:133-225), from opposite-pair sums; deviation storage
+    // starts from the weights' moments.
+    constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
+    float2 rho = add(dup(m0), fr[0]);
+    float2 jx = dup(0.f), jy = jx, jz = jx;
+    float2 sxx = dup(m2), syy = sxx, szz = sxx, sxy = dup(0.f), sxz = sxy, syz = sxy;
+    static_for<0, (QF - 1) / 2>([&](auto KC) {
+      constexpr int L = 2 * decltype(KC)::value + 1;
+      const float2 sp = add(fr[L], fr[L + 1]), dm = sub(fr[L], fr[L + 1]);
+      rho = add(rho, sp);
+      if constexpr (cx(L) != 0) { jx = pk::addsg<cx(L)>(jx, dm); sxx = add(sxx, sp); }
+      if constexpr (cy(L) != 0) { jy = pk::addsg<cy(L)>(jy, dm); syy = add(syy, sp); }
+      if constexpr (cz(L) != 0) { jz = pk::addsg<cz(L)>(jz, dm); szz = add(szz, sp); }
+      if constexpr (cx(L) * cy(L) != 0) sxy = pk::addsg<cx(L) * cy(L)>(sxy, sp);
+      if constexpr (cx(L) * cz(L) != 0) sxz = pk::addsg<cx(L) * cz(L)>(sxz, sp);
+      if constexpr (cy(L) * cz(L) != 0) syz = pk::addsg<cy(L) * cz(L)>(syz, sp);
+    });
+    const float2 inv_rho = make_float2(__frcp_rn(rho.x), __frcp_rn(rho.y));
+    const float2 ux = mul(fma(dup(0.5f), Fx, jx), inv_rho);
+    const float2 uy = mul(fma(dup(0.5f), Fy, jy), inv_rho);
+    const float2 uz = mul(fma(dup(0.5f), Fz, jz), inv_rho);
+    const float2 uF = fma(uz, Fz, fma(uy, Fy, mul(ux, Fx)));
+    const float2 nh = scale(uF, -1.5f);  // -h
+    const float2 nrho = scale(rho, -1.0f);
+    const float2 uxx = mul(ux, ux), uyy = mul(uy, uy), uzz = mul(uz, uz);
+    const float2 uxy = mul(ux, uy), uxz = mul(ux, uz), uyz = mul(uy, uz);
+    // p_ab = s_ab - rho (d_ab / 3 + u_a u_b) + (u_a F_b + u_b F_a) / 2 - h u_a u_b
+    const float2 pxx = fma(nh, uxx, fma(ux, Fx, fma(nrho, add(dup(1.0f / 3.0f), uxx), sxx)));
+    const float2 pyy = fma(nh, uyy, fma(uy, Fy, fma(nrho, add(dup(1.0f / 3.0f), uyy), syy)));
+    const float2 pzz = fma(nh, uzz, fma(uz, Fz, fma(nrho, add(dup(1.0f / 3.0f), uzz), szz)));
+    const float2 pxy = fma(nh, uxy, fma(dup(0.5f), fma(ux, Fy, mul(uy, Fx)), fma(nrho, uxy, sxy)));
+    const float2 pxz = fma(nh, uxz, fma(dup(0.5f), fma(ux, Fz, mul(uz, Fx)), fma(nrho, uxz, sxz)));
+    const float2 pyz = fma(nh, uyz, fma(dup(0.5f), fma(uy, Fz, mul(uz, Fy)), fma(nrho, uyz, syz)));
+    const float2 u2 = add(add(uxx, uyy), uzz);
+    const float2 tr3 = scale(add(add(pxx, pyy), pzz), 1.0f / 3.0f);
+
+    // Regularized collision with He forcing (collisionFluid, src/lbm.cu:233-288):
+    //   f*_l = W_l [E_l (rho + 3/2 (c_l.F - u.F)) + 9/2 (1 - omega) Q_l:Pi]
+    // per opposite pair, with E_l = 1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2.
+    const float2 om = dup((1.0f - omega) * 4.5f);
+    constexpr float fshift = kDevF ? -1.0f : 0.0f;
+    const float2 R = add(rho, nh);
+    const float2 base = fma(dup(-1.5f), u2, dup(1.0f));
+    FT* __restrict__ fo_base = fout + static_cast<long long>(z) * PS + fy0 + fx0;
+    // The shell lanes keep the value the init wrote: f = W (0 in deviation form).
+    auto put = [&](int L, float2 v) {
+      if (sh0 || sh1) {
+        const float wv = kDevF ? 0.0f : wf(L);
+        if (sh0) v.x = wv;
+        if (sh1) v.y = wv;
+      }
+      IO::st2(fo_base + L * 32, v);
+    };
+    {
+      const float2 v = scale(fma(base, R, fma(scale(om, -1.0f), tr3, dup(fshift))), wf(0));
+      put(0, v);
+    }
+    static_for<0, (QF - 1) / 2>([&](auto KC) {
+      constexpr int L = 2 * decltype(KC)::value + 1;
+      constexpr int O = L + 1;
+      constexpr float W = wf(L);
+      float2 cu = dup(0.f), cF = dup(0.f), qp = scale(tr3, -1.0f);
+      if constexpr (cx(L) != 0) { cu = pk::addsg<cx(L)>(cu, ux); cF = pk::addsg<cx(L)>(cF, Fx); qp = add(qp, pxx); }
+      if constexpr (cy(L) != 0) { cu = pk::addsg<cy(L)>(cu, uy); cF = pk::addsg<cy(L)>(cF, Fy); qp = add(qp, pyy); }
+      if constexpr (cz(L) != 0) { cu = pk::addsg<cz(L)>(cu, uz); cF = pk::addsg<cz(L)>(cF, Fz); qp = add(qp, pzz); }
+      if constexpr (cx(L) * cy(L) != 0) qp = fma(dup(2.0f * cx(L) * cy(L)), pxy, qp);
+      if constexpr (cx(L) * cz(L) != 0) qp = fma(dup(2.0f * cx(L) * cz(L)), pxz, qp);
+      if constexpr (cy(L) * cz(L) != 0) qp = fma(dup(2.0f * cy(L) * cz(L)), pyz, qp);
+      const float2 q = fma(om, qp, dup(fshift));
+      const float2 e0 = fma(scale(cu, 4.5f), cu, base), e1 = scale(cu, 3.0f);
+      const float2 rf = scale(cF, 1.5f);
+      put(L, scale(fma(add(e0, e1), add(R, rf), q), W));
+      put(O, scale(fma(sub(e0, e1), sub(R, rf), q), W));
+    });
+
+    // g (collisionPhase, src/lbm.cu:290-329), full relaxation: the populations are the
+    // equilibrium W_l (phi + c_l.J), J = 3 phi u + sharp_c phi (1 - phi) n, pushed as exact
+    // Q2.30 integers into the next phi (streamingCalc + phiCalc).
+    const float2 A = mul(scale(phi, sharp_c), fma(dup(-1.0f), phi, dup(1.0f)));
+    const float2 phi3 = scale(phi, 3.0f);
+    constexpr float kj = 1073741824.0f / 36.0f;
+    const float2 Jx = scale(fma(phi3, ux, mul(A, ncx)), kj);
+    const float2 Jy = scale(fma(phi3, uy, mul(A, ncy)), kj);
+    const float2 Jz = scale(fma(phi3, uz, mul(A, ncz)), kj);
+    // shell lanes push their phi with no flux
+    const JQ j0 = sh0 ? JQ{0, 0, 0}
+                      : JQ{__float2int_rn(Jx.x), __float2int_rn(Jy.x), __float2int_rn(Jz.x)};
+    const JQ j1 = sh1 ? JQ{0, 0, 0}
+                      : JQ{__float2int_rn(Jx.y), __float2int_rn(Jy.y), __float2int_rn(Jz.y)};
+    {
+      const int wf0 = wsplit_face(pc.x), we0 = wsplit_edge_of_face(wf0);
+      const int wf1 = wsplit_face(pc.y), we1 = wsplit_edge_of_face(wf1);
+      auto q0 = [&](auto LC) -> int {
+        constexpr int L = decltype(LC)::value;
+        if constexpr (L == 0) return pc.x - 6 * wf0 - 12 * we0;
+        else return (L <= 6 ? wf0 : we0) + qj<L>(j0);
+      };
+      auto q1 = [&](auto LC) -> int {
+        constexpr int L = decltype(LC)::value;
+        if constexpr (L == 0) return pc.y - 6 * wf1 - 12 * we1;
+        else return (L <= 6 ? wf1 : we1) + qj<L>(j1);
+      };
+      // Ring offsets of the pair's own row in the three target planes.
+      int* s0 = &sacc[(z + 8) & 3][h0];
+      int* sm = &sacc[(z + 7) & 3][h0];
+      int* sp = &sacc[(z + 9) & 3][h0];
+      if (walls && (blo || bhi)) {
+        // A wall plane: what leaves through the wall returns to the cell itself.
+        static_for<0, kQ>([&](auto LC) {
+          constexpr int L = decltype(LC)::value;
+          constexpr int D = cy(L) * HX + cx(L);
+          const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
+          int* tgt = cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0);
+          atomicAdd(bounce ? s0 : tgt + D, q0(LC));
+          atomicAdd(bounce ? s0 + 1 : tgt + D + 1, q1(LC));
+        });
+      } else {
+        // Targets of the pair in one (cy, cz) row: cell x0 reaches h0 - 1 .. h0 + 1, cell
+        // x0 + 1 reaches h0 .. h0 + 2. The two middle targets take one atomic each for
+        // both cells.
+        auto row = [&](int* b, auto LM, auto L0, auto LP) {
+          constexpr int Z = decltype(L0)::value;
+          // LM: cx = -1, L0: cx = 0, LP: cx = +1 (each of the same cy, cz)
+          atomicAdd(b - 1, q0(LM));
+          atomicAdd(b, q0(std::integral_constant<int, Z>{}) + q1(LM));
+          atomicAdd(b + 1, q0(LP) + q1(std::integral_constant<int, Z>{}));
+          atomicAdd(b + 2, q1(LP));
+        };
+        // rest, +x, -x in the cell's own row and plane
+        row(s0, std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
+            std::integral_constant<int, 1>{});
+        // rows y+1 and y-1 in the plane: (-1,+1,0) 14, (0,+1,0) 3, (+1,+1,0) 7;
+        // (-1,-1,0) 8, (0,-1,0) 4, (+1,-1,0) 13
+        row(s0 + HX, std::integral_constant<int, 14>{}, std::integral_constant<int, 3>{},
+            std::integral_constant<int, 7>{});
+        row(s0 - HX, std::integral_constant<int, 8>{}, std::integral_constant<int, 4>{},
+            std::integral_constant<int, 13>{});
+        // planes z+1 and z-1: (-1,0,+1) 16, (0,0,+1) 5, (+1,0,+1) 9;
+        // (-1,0,-1) 10, (0,0,-1) 6, (+1,0,-1) 15
+        row(sp, std::integral_constant<int, 16>{}, std::integral_constant<int, 5>{},
+            std::integral_constant<int, 9>{});
+        row(sm, std::integral_constant<int, 10>{}, std::integral_constant<int, 6>{},
+            std::integral_constant<int, 15>{});
+        // the four (0, +-1, +-1) edges: one target per cell
+        static_for<0, 4>([&](auto KC) {
+          constexpr int K = decltype(KC)::value;
+          constexpr int L = K == 0 ? 11 : (K == 1 ? 12 : (K == 2 ? 17 : 18));
+          constexpr int D = cy(L) * HX;
+          int* b = (cz(L) > 0 ? sp : sm) + D;
+          atomicAdd(b, q0(std::integral_constant<int, L>{}));
+          atomicAdd(b + 1, q1(std::integral_constant<int, L>{}));
+        });
+      }
+    }
+    if (sh0 || sh1) {
+      // The shell's own next phi is the lagged copy of its nearest interior cell
+      // (boundaryConditions, src/lbm.cu:403-425).
+      const int zc = clampi(z, 1, nz - 2) * nxy, yc = clampi(y, 1, ny - 2) * nx;
+      if (sh0) pnext[idx] = __ldg(pcur + clampi(x0, 1, nx - 2) + yc + zc);
+      if (sh1) pnext[idx + 1] = __ldg(pcur + clampi(x0 + 1, 1, nx - 2) + yc + zc);
+    }
+
+    if (a.macros) {
+      const long long T = a.cells_total, o = t.cell_off + idx;
+      float2 mphi = phi, mrho = rho, mx = ux, my = uy, mz = uz;
+      if (sh0) { mphi.x = __int2float_rn(pc.x) * kInvQ30; mrho.x = 1.f; mx.x = my.x = mz.x = 0.f; }
+      if (sh1) { mphi.y = __int2float_rn(pc.y) * kInvQ30; mrho.y = 1.f; mx.y = my.y = mz.y = 0.f; }
+      *reinterpret_cast<float2*>(a.macros + o) = mphi;
+      *reinterpret_cast<float2*>(a.macros + T + o) = mrho;
+      *reinterpret_cast<float2*>(a.macros + 2 * T + o) = mx;
+      *reinterpret_cast<float2*>(a.macros + 3 * T + o) = my;
+      *reinterpret_cast<float2*>(a.macros + 4 * T + o) = mz;
+    }
+  }
+  // The last target planes of the run.
+  __syncthreads();
+  for (int q = max(t.ze - 2, t.zb - 1); q <= t.ze; ++q) flush(q);
+}
+
+// Resident warps per SM of the pair kernel: four blocks of four warps (128 registers).
+constexpr int kPairWarpsPerSM = 16;
+
+template <class S, int BY>
+__global__ void __launch_bounds__(kPairTX * BY, kPairWarpsPerSM * 32 / (kPairTX * BY))
+    k_collide_pair(const StepArgs a) {
+  for_each_segment<2 * kPairTX, BY, true>(
+      a, [&](const Tile& t) { collide_pair_segment<S, BY>(a, t); }, a.balanced != 0);
+}
+
+}  // namespace
+}  // namespace mcb

@@ -37,6 +37,7 @@ EXPORTS = [
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
     "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
     "mcb_checkpoint_save", "mcb_checkpoint_load", "mcb_dump_field", "mcb_get_schedule",
+    "mcb_get_phi_q30",
 ]
 
 
@@ -95,6 +96,7 @@ def lib() -> C.CDLL:
             "mcb_step": [vp, C.c_int],
             "mcb_synchronize": [vp],
             "mcb_get_field": [vp, C.c_int, _FP],
+            "mcb_get_phi_q30": [vp, C.POINTER(C.c_int32)],
             "mcb_diagnostics": [vp, C.POINTER(Diag)],
             "mcb_dump_phi": [vp, C.c_char_p, C.c_char_p, C.c_int],
             "mcb_write_info": [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int,
@@ -272,6 +274,12 @@ class Solver:
         if out is None:
             out = np.empty(self.n, np.float32)
         _check(lib().mcb_get_field(self._h, which, _fptr(out)))
+        return out.reshape(self.shape)
+
+    def get_phi_q30(self) -> np.ndarray:
+        """The exact Q2.30 phi of the latest update (int32, 1.0 = 2^30)."""
+        out = np.empty(self.n, np.int32)
+        _check(lib().mcb_get_phi_q30(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))))
         return out.reshape(self.shape)
 
     def diagnostics(self, allow_nonfinite: bool = False) -> dict:

@@ -145,6 +145,7 @@ def _ref_lib():
                                 C.c_float, C.c_int]
         L.ref_set_phi.argtypes = [C.c_void_p, _FP]
         L.ref_run.argtypes = [C.c_void_p, C.c_int, _FP]
+        L.ref_run_streams.argtypes = [C.c_void_p, C.c_int, C.c_int, _FP]
         L.ref_get.argtypes = [C.c_void_p, C.c_int, _FP]
         L.ref_close.argtypes = [C.c_void_p]
         _ref = L
@@ -169,9 +170,11 @@ class ReferenceKernels:
         if _ref_lib().ref_set_phi(self._h, a.ctypes.data_as(_FP)):
             raise RuntimeError(_ref_lib().ref_error().decode())
 
-    def run(self, nsteps) -> float:
+    def run(self, nsteps, streams=1) -> float:
+        """nsteps updates; streams=3 issues the two collisions on their own streams, as the
+        reference's main loop does (src/main.cu:127-141). Returns the device milliseconds."""
         ms = C.c_float()
-        if _ref_lib().ref_run(self._h, nsteps, C.byref(ms)):
+        if _ref_lib().ref_run_streams(self._h, nsteps, streams, C.byref(ms)):
             raise RuntimeError(_ref_lib().ref_error().decode())
         return ms.value
 

@@ -59,14 +59,19 @@ struct Ref {
   CUfunction k[kNumK] = {};
   CUdeviceptr a[kNumA] = {};
   CUstream stream = nullptr;
+  // The reference's own stream layout (src/main.cu:49-52): collisionFluid and
+  // collisionPhase on two more streams, created with default flags, not ordered after the
+  // kernels of the main stream (src/main.cu:127-141). Only ref_run_streams(..., 3) uses them.
+  CUstream coll_fluid = nullptr, coll_phase = nullptr;
   CUevent e0 = nullptr, e1 = nullptr;
   int NX = 0, NY = 0, NZ = 0;
   int moving_wall = 1;
 
-  int launch(K which, std::vector<void*> args) {
+  int launch(K which, std::vector<void*> args, CUstream on = nullptr) {
     const unsigned bx = 8, by = 8, bz = 8;
     const unsigned gx = (NX + 7) / 8, gy = (NY + 7) / 8, gz = (NZ + 7) / 8;
-    RH(cuLaunchKernel(k[which], gx, gy, gz, bx, by, bz, 0, stream, args.data(), nullptr));
+    RH(cuLaunchKernel(k[which], gx, gy, gz, bx, by, bz, 0, on ? on : stream, args.data(),
+                      nullptr));
     return 0;
   }
 };
@@ -191,12 +196,22 @@ int ref_set_phi(void* h, const float* phi) {
   return 0;
 }
 
-// The body of the step loop (src/main.cu:79-178) nsteps times on one stream, timed with
-// events around the launches.
-int ref_run(void* h, int nsteps, float* ms) {
+// The body of the step loop (src/main.cu:79-178) nsteps times, timed with events around
+// the launches. streams = 1: every kernel on one stream, in the intended order. streams = 3:
+// the reference's own layout, collisionFluid and collisionPhase on two more streams with no
+// dependency on momentiCalc, then both streams synchronised from the host
+// (src/main.cu:127-141). That order races; its results vary from run to run, which sets the
+// noise floor of any comparison with the reference.
+int ref_run_streams(void* h, int nsteps, int streams, float* ms) {
   Ref* r = static_cast<Ref*>(h);
-  if (!r || !r->NX || nsteps < 0) return 1;
+  if (!r || !r->NX || nsteps < 0 || (streams != 1 && streams != 3)) return 1;
   RH(cuCtxSetCurrent(r->ctx));
+  if (streams == 3 && !r->coll_fluid) {
+    RH(cuStreamCreate(&r->coll_fluid, CU_STREAM_DEFAULT));
+    RH(cuStreamCreate(&r->coll_phase, CU_STREAM_DEFAULT));
+  }
+  CUstream sf = streams == 3 ? r->coll_fluid : nullptr;
+  CUstream sp = streams == 3 ? r->coll_phase : nullptr;
   int NX = r->NX, NY = r->NY, NZ = r->NZ;
   CUdeviceptr* a = r->a;
   RH(cuEventRecord(r->e0, r->stream));
@@ -210,16 +225,22 @@ int ref_run(void* h, int nsteps, float* ms) {
                                  &a[aPxz], &a[aPyz], &NX, &NY, &NZ}) ||
         r->launch(kCollisionFluid, {&a[aF], &a[aUx], &a[aUy], &a[aUz], &a[aFfx], &a[aFfy],
                                     &a[aFfz], &a[aRho], &a[aPxx], &a[aPyy], &a[aPzz],
-                                    &a[aPxy], &a[aPxz], &a[aPyz], &NX, &NY, &NZ}) ||
+                                    &a[aPxy], &a[aPxz], &a[aPyz], &NX, &NY, &NZ}, sf) ||
         r->launch(kCollisionPhase, {&a[aG], &a[aUx], &a[aUy], &a[aUz], &a[aPhi], &a[aNx],
-                                    &a[aNy], &a[aNz], &NX, &NY, &NZ}))
+                                    &a[aNy], &a[aNz], &NX, &NY, &NZ}, sp))
       return 1;
+    if (streams == 3) {
+      RH(cuStreamSynchronize(sf));
+      RH(cuStreamSynchronize(sp));
+    }
     if (r->moving_wall && r->launch(kMovingWallBC, {&a[aF], &a[aRho], &NX, &NY, &NZ})) return 1;
     if (r->launch(kStreamingCalc, {&a[aG], &a[aGout], &NX, &NY, &NZ})) return 1;
     std::swap(a[aG], a[aGout]);
     if (r->launch(kFgBoundary, {&a[aF], &a[aRho], &a[aG], &a[aPhi], &NX, &NY, &NZ}) ||
         r->launch(kBoundaryConditions, {&a[aPhi], &NX, &NY, &NZ}))
       return 1;
+    // src/main.cu:180 waits for the device after every update
+    if (streams == 3) RH(cuCtxSynchronize());
   }
   RH(cuEventRecord(r->e1, r->stream));
   RH(cuEventSynchronize(r->e1));
@@ -228,6 +249,8 @@ int ref_run(void* h, int nsteps, float* ms) {
   if (ms) *ms = t;
   return 0;
 }
+
+int ref_run(void* h, int nsteps, float* ms) { return ref_run_streams(h, nsteps, 1, ms); }
 
 // which: 0 phi, 1 rho, 2 ux, 3 uy, 4 uz
 int ref_get(void* h, int which, float* host) {
@@ -251,6 +274,8 @@ void ref_close(void* h) {
   if (r->e0) cuEventDestroy(r->e0);
   if (r->e1) cuEventDestroy(r->e1);
   if (r->stream) cuStreamDestroy(r->stream);
+  if (r->coll_fluid) cuStreamDestroy(r->coll_fluid);
+  if (r->coll_phase) cuStreamDestroy(r->coll_phase);
   if (r->mod) cuModuleUnload(r->mod);
   cuDevicePrimaryCtxRelease(r->dev);
   delete r;

@@ -9,7 +9,10 @@ for p in (str(REPO), str(PKG)):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REFERENCE_POST = Path("/root/reference/post")
+# The reference checkout (read-only), if present: REF_ROOT, as in oracle/build.py.
+from oracle.build import DEFAULT_REF_ROOT  # noqa: E402
+
+REFERENCE_POST = DEFAULT_REF_ROOT / "post"
 
 
 def pytest_configure(config):

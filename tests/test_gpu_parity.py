@@ -236,18 +236,114 @@ def test_tma_collide_is_skipped_where_it_does_not_apply():
         assert s.schedule[0] == 0
 
 
+PAIR = 5  # the two-cells-per-thread tile variant
+
+
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
 def test_work_splits_agree_bitwise_with_equilibrium_g(storage):
     """Balanced ranges (pieces that start mid-column and span columns) and fixed chunks
-    give the same fields, bit for bit."""
+    give the same fields, bit for bit: every one-cell tile variant, and the pair kernel
+    against itself."""
     cfg, phi, u = small_case(mcb.BC_WALLS_Z, n=(72, 40, 96), gravity=1e-4, noise=1e-3)
     cfg.storage = storage
-    base = gpu_run(cfg, phi, u, steps=23, variant=0, zchunk=5)
+    base = {0: gpu_run(cfg, phi, u, steps=23, variant=0, zchunk=5),
+            PAIR: gpu_run(cfg, phi, u, steps=23, variant=PAIR, zchunk=5)}
     for v in range(mcb.lib().mcb_variant_count()):
         for zc in (0, -1, -2, -7, 16):
             r = gpu_run(cfg, phi, u, steps=23, variant=v, zchunk=zc)
+            want = base[PAIR if v == PAIR else 0]
             for k in FIELDS:
-                assert np.array_equal(r[k], base[k]), (v, zc, k)
+                assert np.array_equal(r[k], want[k]), (v, zc, k)
+
+
+# |pair kernel - one-cell kernel| after 31 updates: the same arithmetic with the fused
+# multiply-adds placed differently, so the fields part at FP32 rounding; 16-bit storage
+# rounds each stored population, which a last-bit difference can move by one 16-bit unit.
+PAIR_TOL = {mcb.STORE_F32: {"phi": 2e-6, "rho": 2e-6, "ux": 2e-7, "uy": 2e-7, "uz": 2e-7},
+            mcb.STORE_F16: {"phi": 2e-5, "rho": 2e-5, "ux": 2e-6, "uy": 2e-6, "uz": 2e-6},
+            mcb.STORE_BF16: {"phi": 2e-4, "rho": 2e-4, "ux": 2e-5, "uy": 2e-5, "uz": 2e-5}}
+
+
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
+@pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z, mcb.BC_REF])
+def test_pair_kernel_matches_the_one_cell_kernel(bc, storage):
+    """The two-cells-per-thread collide against the one-cell collide: partial tiles in x
+    (nx = 72 is not a multiple of the 64-cell tile) and y, walls with gravity, periodic
+    images, reference shells (pairs that hold a shell cell and an interior cell)."""
+    if bc == mcb.BC_REF:
+        cfg, u = reference_cfg(32), None
+        cfg.nx, cfg.ny, cfg.nz = 72, 22, 30
+        phi = mcb.fill_phi_bubbles(72, 22, 30, bc, 4.0, [(30.3, 10.6, 14.1, 7.0)])
+    else:
+        cfg, phi, u = small_case(bc, n=(72, 22, 30), gravity=1e-4, noise=1e-3)
+    cfg.storage = storage
+    runs = {}
+    for v in (PAIR, 0):
+        cfg.variant = v
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, *(u if u is not None else (None, None, None)))
+            assert s.schedule[0] == v
+            s.step(1)
+            m0 = s.diagnostics()["mass_q30"]
+            s.step(30)
+            runs[v] = {k: s.get(k).astype(np.float64) for k in FIELDS}
+            if bc != mcb.BC_REF:
+                assert s.diagnostics()["mass_q30"] == m0, v
+    for k, tol in PAIR_TOL[storage].items():
+        assert maxdiff(runs[PAIR], runs[0], k) < tol, (k, maxdiff(runs[PAIR], runs[0], k))
+
+
+@pytest.mark.parametrize("bc,gravity,noise", [(mcb.BC_PERIODIC, 0.0, 0.0),
+                                              (mcb.BC_PERIODIC, 1e-4, 1e-3),
+                                              (mcb.BC_WALLS_Z, 1e-4, 1e-3)])
+def test_pair_kernel_matches_fp64_oracle(bc, gravity, noise):
+    cfg, phi, u = small_case(bc, gravity=gravity, noise=noise)
+    g = gpu_run(cfg, phi, u, steps=30, variant=PAIR)
+    o = oracle_run(cfg, phi, u, steps=30)
+    for k, tol in TOL.items():
+        assert maxdiff(g, o, k) < tol, (k, maxdiff(g, o, k))
+
+
+def test_pair_kernel_in_reference_mode_matches_reference_kernels():
+    if not harness_available():
+        pytest.skip("reference cubin not built")
+    n = 32
+    cfg = reference_cfg(n)
+    phi = off_centre_reference_phi(n)
+    ref = _reference_kernels(cfg, phi, 300)
+    g = gpu_run(cfg, phi, steps=300, variant=PAIR)
+    inner = (slice(1, -1),) * 3
+    for k in FIELDS:
+        d = float(np.max(np.abs(g[k][inner] - ref[k][inner])))
+        assert d < TOL[k], (k, d)
+
+
+def test_pair_kernel_is_skipped_where_it_does_not_apply():
+    # odd nx, stored relaxed g, D3Q27 f, a density ratio: the one-cell 32x8 tile runs
+    for over in ({"n": (23, 20, 28)}, {"tau_g": 0.8}, {"velocity_set": 27}, {"rho_in": 10.0}):
+        kw = {k: v for k, v in over.items() if k in ("n", "tau_g")}
+        cfg, phi, u = small_case(mcb.BC_PERIODIC, **kw)
+        for k, v in over.items():
+            if k not in ("n", "tau_g"):
+                setattr(cfg, k, v)
+        cfg.variant = PAIR
+        with mcb.Solver(cfg) as s:
+            assert s.schedule[0] == 0, over
+
+
+def test_pair_kernel_with_64bit_plane_offsets_agrees_bitwise(monkeypatch):
+    """The pair kernel addresses f per plane with 64-bit offsets, so cases that need 64-bit
+    f offsets run it on the blocked layout. MCB_WIDE_OFFSETS=1 forces that path on a small
+    case: the fields must not change."""
+    cfg, phi, u = small_case(mcb.BC_WALLS_Z, gravity=1e-4, noise=1e-3)
+    base = gpu_run(cfg, phi, u, steps=23, variant=PAIR)
+    monkeypatch.setenv("MCB_WIDE_OFFSETS", "1")
+    cfg.variant = PAIR
+    with mcb.Solver(cfg) as s:
+        assert s.schedule[0] == PAIR
+    wide = gpu_run(cfg, phi, u, steps=23, variant=PAIR)
+    for k in FIELDS:
+        assert np.array_equal(wide[k], base[k]), k
 
 
 @pytest.mark.parametrize("velocity_set,ratio,tau_g", [(19, 1.0, 1.0), (19, 1.0, 0.8),

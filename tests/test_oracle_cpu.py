@@ -263,3 +263,26 @@ def test_density_ratio_is_refused_in_reference_mode(built):
     c = mcb.default_config(rho_in=10.0, rho_out=1.0)
     with pytest.raises(mcb.McbError, match="density-matched"):
         mcb.Solver(c)
+
+
+@pytest.mark.parametrize("scale", [0.25, 0.5])
+def test_oracle_side_generator_matches_the_solver_workload(built, scale):
+    """The benchmark's CPU reference arm builds the rising-bubble field without the solver
+    library (oracle/workload_port.py). It must be the field the solver generates."""
+    from oracle.workload_port import rising_bubble
+
+    cfg, phi, ux, uy, uz = mcb.workload(2, seed=1, scale=scale)
+    mine, p = rising_bubble(seed=1, scale=scale)
+    assert mine.shape == phi.shape == (cfg.nz, cfg.ny, cfg.nx)
+    assert (p["nx"], p["ny"], p["nz"], p["bc"]) == (cfg.nx, cfg.ny, cfg.nz, cfg.bc)
+    assert np.float32(p["tau"]) == cfg.tau and np.float32(p["sigma"]) == cfg.sigma
+    assert np.float32(p["gravity"]) == cfg.gravity and p["width"] == cfg.width
+    # libm and numpy may round a transcendental differently in the last double bit. That
+    # can move a float32 value by one unit in the last place, or, deep in the tanh tail,
+    # leave 1e-16 where the other rounds to exactly 0.
+    d = np.abs(mine.astype(np.float64) - phi)
+    assert d.max() <= 1e-15 or d.max() <= 2 * np.finfo(np.float32).eps, d.max()
+    big = np.maximum(mine, phi) > 1e-6
+    ulps = np.abs(mine.view(np.int32).astype(np.int64) - phi.view(np.int32).astype(np.int64))
+    assert ulps[big].max() <= 2, ulps[big].max()
+    assert not ux.any() and not uy.any() and not uz.any()
