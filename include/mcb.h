@@ -203,7 +203,9 @@ int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_s
                          double fy, double fz, int save_every, int nsteps, double mlups);
 
 /* The tile variant and z chunk setting the handle runs (after defaults and autotuning).
- * variant 4 is the TMA-staged 32x8 collide on the padded f layout. */
+ * variant 4 is the TMA-staged 32x8 collide on the padded f layout; variant 5 takes two
+ * neighbouring cells in x per thread (64x4 cells per block, equilibrium g with D3Q19 f at
+ * density ratio 1 and an even nx; elsewhere a request for it runs variant 0). */
 int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
 
 /* Checkpoint and restart. No counterpart in the reference, which saves only phi
@@ -325,6 +327,25 @@ int  mcb_batch_diagnostics(mcb_batch* b, int case_index, mcb_diag* out);
 int  mcb_batch_last_step_ms(mcb_batch* b, float* ms);
 /* Total lattice cells over all cases (for MLUPS). */
 int  mcb_batch_cells(const mcb_batch* b, int64_t* cells);
+
+/* Per-size-class tile choice for a batch. The reference launches every kernel with one fixed
+ * 8x8x8 block shape (src/main.cu:43-46); here a batch can pick, for each size class (the
+ * cases of one nx, ny, nz), the tile variant and z chunk that run that class fastest.
+ * On a copy of the batch's state, for nsteps updates per trial, it times:
+ *   - the untuned schedule (every case in one launch, the batch's variant and split);
+ *   - each size class alone with every tile variant that fits and the z chunks
+ *     0 (default), 8, 16, 24, 32, 48, 64;
+ *   - the chosen classes combined: one launch per chosen variant, each case with its
+ *     class's chunk, and one launch of every case with the variant that covers the most
+ *     cells.
+ * It keeps the fastest measured combination (or the untuned schedule if none beats it),
+ * reports both MLUPS, and restores the fields. Results do not depend on the work split;
+ * the one-cell tile variants give identical fields, and the two-cells-per-thread variant
+ * agrees with them to FP32 rounding. */
+int  mcb_batch_autotune(mcb_batch* b, int nsteps, double* default_mlups, double* tuned_mlups);
+
+/* The tile variant and z chunk setting that case case_index of a batch runs. */
+int  mcb_batch_get_schedule(const mcb_batch* b, int case_index, int* variant, int* zchunk);
 
 #ifdef __cplusplus
 }

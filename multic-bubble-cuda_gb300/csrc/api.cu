@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -147,8 +148,21 @@ struct Solver {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaGraphExec_t graph[8] = {};  // per (f parity, phi slot) at the start of the graph
   int graph_steps = 16;
-  int ntiles = 0, zchunk = 16;
-  int balanced = 1, phi_balanced = 0, planes = 0, grid_phi = 0, grid_collide = 0;
+  // Launch groups: the cases of each group run one phi and one collide launch per update,
+  // with the group's tile variant. A single case, and a batch until mcb_batch_autotune
+  // splits it, is one group of every case with the handle's variant and z chunk request.
+  struct Group {
+    int variant = 0, zchunk_req = 0;
+    std::vector<int> members;  // case indices, in launch order
+    std::vector<int> zc_case;  // per member: > 0 fixed z chunk overriding the group's split
+    int ntiles = 0, zchunk = 16, balanced = 1, phi_balanced = 0, planes = 0;
+    int grid_phi = 0, grid_collide = 0;
+    int table = 0;  // first entry of the group's case table in d_gcases
+  };
+  std::vector<Group> groups;
+  bool grouped = false;  // groups set by the batch autotuner (else one group, rebuilt)
+  mcb::CaseDesc* d_gcases = nullptr;  // the case tables of the groups, back to back
+  std::vector<mcb::CaseDesc> gtab;    // host image of d_gcases
   int parity = 0, first = 1, latest_p = 1;
   int pk = 0;  // current phi buffer; advances by one per update, modulo nphi()
   long long update = -1;
@@ -196,6 +210,8 @@ struct Solver {
     cudaFree(partials);
     cudaFree(result);
     cudaFree(d_cases);
+    cudaFree(d_gcases);
+    d_gcases = nullptr;
     macros = stage = nullptr;
     partials = result = nullptr;
     d_cases = nullptr;
@@ -208,35 +224,30 @@ struct Solver {
     stream = nullptr;
   }
 
-  // Work decomposition of every case for the current variant and z chunk request:
+  // Work decomposition of the cases of one group for its variant and z chunk request:
   //   zchunk_req > 0: fixed chunks of that many planes, one block each;
   //   zchunk_req < 0: balanced ranges, -zchunk_req resident waves of equal-work blocks
   //   per kernel;
   //   zchunk_req == 0: fixed chunks chosen below.
-  int build_tiles() {
-    const mcb::Variant v = mcb::kVariants[variant];
+  // A member's own fixed chunk (zc_case > 0) overrides the group's unless it is balanced.
+  int build_group(Group& g, int nsm) {
+    const mcb::Variant v = mcb::kVariants[g.variant];
     long long plane_total = 0;
-    for (auto& d : cases) {
+    for (int ci : g.members) {
+      mcb::CaseDesc& d = cases[ci];
       d.tiles_x = (d.nx + v.bx - 1) / v.bx;
       d.tiles_y = (d.ny + v.by - 1) / v.by;
       d.plane0 = static_cast<int>(plane_total);
       plane_total += static_cast<long long>(d.tiles_x) * d.tiles_y * d.nz;
       if (plane_total > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tile planes");
     }
-    planes = static_cast<int>(plane_total);
-    balanced = zchunk_req < 0;
-    int nsm = 0, occ_phi = 0, occ_col = 0;
-    MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-    MCB_CU(mcb::occupancy(storage, variant, gmode, qf, ratio, wide, &occ_phi, &occ_col));
-    if (nsm <= 0 || occ_phi <= 0 || occ_col <= 0)
-      return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", variant);
-    auto tiles_for = [&](int zc) {
-      long long total = 0;
-      for (auto& d : cases)
-        total += static_cast<long long>(d.tiles_x) * d.tiles_y * ((d.nz + zc - 1) / zc);
-      return total;
-    };
-    int zc = zchunk_req;
+    g.planes = static_cast<int>(plane_total);
+    g.balanced = g.zchunk_req < 0;
+    int occ_phi = 0, occ_col = 0;
+    MCB_CU(mcb::occupancy(storage, g.variant, gmode, qf, ratio, wide, &occ_phi, &occ_col));
+    if (occ_phi <= 0 || occ_col <= 0)
+      return fail(MCB_ERR_CUDA, "no resident blocks for tile variant %d", g.variant);
+    int zc = g.zchunk_req;
     if (zc <= 0) {
       // Default split, from sweeps on GB300: when one case's tile columns fit in one
       // resident wave of collide blocks, cut every column into the same number of chunks so
@@ -247,52 +258,96 @@ struct Solver {
       const long long wave = 1LL * occ_col * nsm;
       long long cols = 0;
       int nzmax = 1;
-      for (auto& d : cases) {
-        cols += static_cast<long long>(d.tiles_x) * d.tiles_y;
-        nzmax = std::max(nzmax, d.nz);
+      for (int ci : g.members) {
+        cols += static_cast<long long>(cases[ci].tiles_x) * cases[ci].tiles_y;
+        nzmax = std::max(nzmax, cases[ci].nz);
       }
-      if (cases.size() == 1 && cols <= wave) {
+      if (g.members.size() == 1 && cols <= wave) {
         const long long m = std::max<long long>(1, std::min<long long>(wave / cols, nzmax / 8));
         zc = static_cast<int>((nzmax + m - 1) / m);
       } else {
         zc = 32;
       }
     }
-    const long long tile0_total = tiles_for(zc);
-    if (tile0_total > 0x7fffffffLL)
-      return fail(MCB_ERR_INVALID, "too many tiles (%lld)", tile0_total);
     long long tile0 = 0;
-    for (auto& d : cases) {
-      d.zchunk = zc;
-      d.tiles_z = (d.nz + zc - 1) / zc;
+    for (size_t k = 0; k < g.members.size(); ++k) {
+      mcb::CaseDesc& d = cases[g.members[k]];
+      const int own = k < g.zc_case.size() ? g.zc_case[k] : 0;
+      d.zchunk = (own > 0 && !g.balanced) ? own : zc;
+      d.tiles_z = (d.nz + d.zchunk - 1) / d.zchunk;
       d.tile0 = static_cast<int>(tile0);
       tile0 += static_cast<long long>(d.tiles_x) * d.tiles_y * d.tiles_z;
+      if (tile0 > 0x7fffffffLL) return fail(MCB_ERR_INVALID, "too many tiles (%lld)", tile0);
     }
-    ntiles = static_cast<int>(tile0);
-    zchunk = balanced ? zchunk_req : zc;
-    phi_balanced = 0;
-    if (balanced) {
-      const int waves = -zchunk;
-      grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm * waves));
+    g.ntiles = static_cast<int>(tile0);
+    g.zchunk = g.balanced ? g.zchunk_req : zc;
+    g.phi_balanced = 0;
+    if (g.balanced) {
+      const int waves = -g.zchunk;
+      g.grid_phi = static_cast<int>(std::min<long long>(g.planes, 1LL * occ_phi * nsm * waves));
       // A collide piece re-reads four phi planes and recomputes two normal planes before
       // its first plane: give each block at least kMinCollidePlanes.
-      grid_collide = static_cast<int>(std::min<long long>(
-          std::max(1, planes / kMinCollidePlanes), 1LL * occ_col * nsm * waves));
+      g.grid_collide = static_cast<int>(std::min<long long>(
+          std::max(1, g.planes / kMinCollidePlanes), 1LL * occ_col * nsm * waves));
     } else {
-      grid_phi = grid_collide = ntiles;
+      g.grid_phi = g.grid_collide = g.ntiles;
       // When the collide chunks leave part of a phi wave idle, the record phi kernel (no
       // halo to prime) takes one resident wave of equal runs instead: 128x128x256 57 us
       // against 59, with the D3Q27 chunks 57 against 87. Larger cases keep the chunks
       // (512^3: 1.47 ms against 1.74 balanced).
-      phi_balanced = gmode == mcb::kGEquil && ntiles < 1LL * occ_phi * nsm;
-      if (phi_balanced)
-        grid_phi = static_cast<int>(std::min<long long>(planes, 1LL * occ_phi * nsm));
+      g.phi_balanced = gmode == mcb::kGEquil && g.ntiles < 1LL * occ_phi * nsm;
+      if (g.phi_balanced)
+        g.grid_phi = static_cast<int>(std::min<long long>(g.planes, 1LL * occ_phi * nsm));
     }
+    return MCB_OK;
+  }
+
+  // Rebuilds the work decomposition of every group (one group of every case with the
+  // handle's variant and z chunk request, unless the batch autotuner set the groups).
+  int build_tiles() {
+    if (!grouped) {
+      groups.assign(1, Group{});
+      groups[0].variant = variant;
+      groups[0].zchunk_req = zchunk_req;
+      for (int i = 0; i < static_cast<int>(cases.size()); ++i) groups[0].members.push_back(i);
+    }
+    int nsm = 0;
+    MCB_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    if (nsm <= 0) return fail(MCB_ERR_CUDA, "no multiprocessors");
+    for (auto& g : groups) MCB_TRY(build_group(g, nsm));
     drop_graphs();
-    MCB_CU(cudaMemcpyAsync(d_cases, cases.data(), sizeof(mcb::CaseDesc) * cases.size(),
-                           cudaMemcpyHostToDevice, stream));
+    MCB_TRY(upload_tables());
     MCB_CU(cudaStreamSynchronize(stream));
     return MCB_OK;
+  }
+
+  // The case table in case order (init, diagnostics) and the groups' launch tables.
+  int upload_tables() {
+    gtab.clear();
+    for (auto& g : groups) {
+      g.table = static_cast<int>(gtab.size());
+      for (int ci : g.members) gtab.push_back(cases[ci]);
+    }
+    MCB_CU(cudaMemcpyAsync(d_cases, cases.data(), sizeof(mcb::CaseDesc) * cases.size(),
+                           cudaMemcpyHostToDevice, stream));
+    MCB_CU(cudaMemcpyAsync(d_gcases, gtab.data(), sizeof(mcb::CaseDesc) * gtab.size(),
+                           cudaMemcpyHostToDevice, stream));
+    return MCB_OK;
+  }
+
+  // The schedule of case ci: its group's variant, and its z chunk setting (the group's
+  // request, or the case's own fixed chunk).
+  void schedule_of(int ci, int* v, int* zc) const {
+    for (const auto& g : groups)
+      for (size_t k = 0; k < g.members.size(); ++k)
+        if (g.members[k] == ci) {
+          *v = g.variant;
+          const int own = k < g.zc_case.size() ? g.zc_case[k] : 0;
+          *zc = (own > 0 && !g.balanced) ? own : g.zchunk;
+          return;
+        }
+    *v = variant;
+    *zc = zchunk_req;
   }
 
   int create(const mcb_config* cs, int n) {
@@ -364,12 +419,12 @@ struct Solver {
     // cases that need 64-bit f offsets, on the blocked layout.
     pair_ok = gmode == mcb::kGEquil && qf == 19 && !ratio && !padded;
     for (auto& d : cases) pair_ok = pair_ok && d.nx % 2 == 0;
-    if (variant == mcb::kPairVariant && !pair_ok) variant = 0;
+    if (mcb::is_pair_variant(variant) && !pair_ok) variant = 0;
     // f layout: blocked with equilibrium g and 32-bit offsets (x rounded up to whole 32-cell
     // blocks), or with the pair kernel at any size; plain otherwise (the 64-bit one-cell
     // kernels and the stored-g ones measured slower blocked: they spill the extra per-thread
     // offsets). The padded TMA layout is set below.
-    const bool blocked = gmode == mcb::kGEquil && (!wide || variant == mcb::kPairVariant);
+    const bool blocked = gmode == mcb::kGEquil && (!wide || mcb::is_pair_variant(variant));
     wide_blocked = wide && blocked;
     f_cells_total = max_f_cells = 0;
     for (auto& d : cases) {
@@ -424,6 +479,7 @@ struct Solver {
     MCB_CU(cudaMalloc(&partials, sizeof(mcb::DiagPartial) * mcb::kDiagBlocks));
     MCB_CU(cudaMalloc(&result, sizeof(mcb::DiagPartial)));
     MCB_CU(cudaMalloc(&d_cases, sizeof(mcb::CaseDesc) * n));
+    MCB_CU(cudaMalloc(&d_gcases, sizeof(mcb::CaseDesc) * n));
     MCB_CU(cudaMalloc(&err, sizeof(int)));
     MCB_CU(cudaMemset(err, 0, sizeof(int)));
     if (padded) {
@@ -431,6 +487,32 @@ struct Solver {
       for (int i = 0; i < 2; ++i) MCB_TRY(encode_fmap(i));
     }
     return build_tiles();
+  }
+
+  // Whether tile variant v can run these cases on the f layout fixed at creation: the TMA
+  // variant alone on the padded layout; D3Q27 f and the density-ratio model on the 32x8
+  // tile; the pair kernel where it applies, and alone on a blocked layout with 64-bit
+  // offsets.
+  bool variant_fits(int v) const {
+    if ((v == mcb::kTmaVariant) != padded) return false;
+    if ((qf == 27 || ratio) && v != 0) return false;
+    if (mcb::is_pair_variant(v) && !pair_ok) return false;
+    if (wide_blocked && !mcb::is_pair_variant(v)) return false;
+    return true;
+  }
+
+  // Runs 2 updates to warm up (graph captures included), then nsteps timed ones; reports
+  // the MLUPS of the cases the groups hold.
+  int time_updates(int nsteps, double* mlups) {
+    MCB_TRY(step(2));
+    MCB_TRY(step(nsteps));
+    float ms = 0.f;
+    MCB_TRY(last_ms(&ms));
+    long long cells = 0;
+    for (const auto& gr : groups)
+      for (int ci : gr.members) cells += cases[ci].ncell;
+    *mlups = static_cast<double>(cells) * nsteps / (ms * 1e-3) / 1e6;
+    return MCB_OK;
   }
 
   size_t f_bytes() const {
@@ -514,7 +596,7 @@ struct Solver {
       MCB_CU(cudaMemcpyAsync(stage + 3 * n, uz, n * sizeof(float), cudaMemcpyHostToDevice,
                              stream));
     }
-    MCB_CU(cudaMemcpyAsync(d_cases + ci, &d, sizeof d, cudaMemcpyHostToDevice, stream));
+    MCB_TRY(upload_tables());
     // A single case restarts from update 0 in buffer set 0.
     if (cases.size() == 1 || !stepped) {
       parity = 0;
@@ -549,16 +631,17 @@ struct Solver {
     return MCB_OK;
   }
 
-  mcb::StepArgs args(bool with_macros) const {
+  mcb::StepArgs args(const Group& gr, bool with_macros) const {
     mcb::StepArgs a{};
-    a.cases = d_cases;
-    a.ncases = static_cast<int>(cases.size());
-    a.ntiles = ntiles;
-    a.balanced = balanced;
-    a.phi_balanced = balanced || phi_balanced;
-    a.planes = planes;
-    a.grid_phi = grid_phi;
-    a.grid_collide = grid_collide;
+    a.cases = d_gcases + gr.table;
+    a.ncases = static_cast<int>(gr.members.size());
+    for (int ci : gr.members) a.has_ref = a.has_ref || cases[ci].bc == mcb::kBcRef;
+    a.ntiles = gr.ntiles;
+    a.balanced = gr.balanced;
+    a.phi_balanced = gr.balanced || gr.phi_balanced;
+    a.planes = gr.planes;
+    a.grid_phi = gr.grid_phi;
+    a.grid_collide = gr.grid_collide;
     a.err = err;
     a.qf = qf;
     a.ratio = ratio;
@@ -590,9 +673,20 @@ struct Solver {
     return gmode == mcb::kGEquil ? (push || first) : (push && !first);
   }
 
-  // The phi stage of an update: the phi kernel, or nothing (push, first equilibrium update).
-  int launch_phi_stage(const mcb::StepArgs& a) {
-    if (!skips_phi()) MCB_CU(mcb::launch_phi(storage, variant, gmode, a, stream));
+  // The phi stage of an update: the phi kernels of the groups, or nothing (push, first
+  // equilibrium update).
+  int launch_phi_stage(bool with_macros) {
+    if (skips_phi()) return MCB_OK;
+    for (const auto& gr : groups)
+      MCB_CU(mcb::launch_phi(storage, gr.variant, gmode, args(gr, with_macros), stream));
+    return MCB_OK;
+  }
+
+  // The collide kernels of the groups.
+  int launch_collide_stage(bool with_macros) {
+    for (const auto& gr : groups)
+      MCB_CU(mcb::launch_collide(storage, gr.variant, gmode, args(gr, with_macros),
+                                 padded ? &fmap[parity] : nullptr, stream));
     return MCB_OK;
   }
 
@@ -606,10 +700,8 @@ struct Solver {
   }
 
   int launch_update(bool with_macros) {
-    const mcb::StepArgs a = args(with_macros);
-    MCB_TRY(launch_phi_stage(a));
-    MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
-                               stream));
+    MCB_TRY(launch_phi_stage(with_macros));
+    MCB_TRY(launch_collide_stage(with_macros));
     advance();
     return MCB_OK;
   }
@@ -688,11 +780,9 @@ struct Solver {
     MCB_CU(cudaEventRecord(prof_events[0], stream));
     MCB_CU(cudaEventRecord(ev0, stream));
     for (int i = 0; i < nsteps; ++i) {
-      const mcb::StepArgs a = args(i == nsteps - 1);
-      MCB_TRY(launch_phi_stage(a));
+      MCB_TRY(launch_phi_stage(i == nsteps - 1));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 1], stream));
-      MCB_CU(mcb::launch_collide(storage, variant, gmode, a, padded ? &fmap[parity] : nullptr,
-                               stream));
+      MCB_TRY(launch_collide_stage(i == nsteps - 1));
       MCB_CU(cudaEventRecord(prof_events[2 * i + 2], stream));
       advance();
     }
@@ -841,7 +931,8 @@ struct Solver {
     pk = push ? hd.pk : parity;
     update = hd.update;
     d.phi_mean = hd.phi_mean;
-    MCB_CU(cudaMemcpy(d_cases, &d, sizeof d, cudaMemcpyHostToDevice));
+    MCB_TRY(upload_tables());
+    MCB_CU(cudaStreamSynchronize(stream));
     drop_graphs();
     fields_set[0] = 1;
     stepped = update >= 0;
@@ -960,6 +1051,83 @@ int report_error(int code, const char* msg) {
   return code;
 }
 }  // namespace mcb
+
+// A copy of the state the next update reads, so that timing trials can run on the live
+// fields and leave them as they were. Owns its device copies.
+struct StateCopy {
+  Solver& s;
+  void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
+  size_t n = 0, fb = 0, gb = 0;
+  int par = 0, first = 0, latest = 0, pk = 0;
+  long long update = -1;
+  bool eq = false;
+
+  explicit StateCopy(Solver& solver) : s(solver) {}
+  ~StateCopy() {
+    cudaFree(fs);
+    cudaFree(gs);
+    cudaFree(rs);
+    cudaFree(ps);
+    cudaFree(ms);
+  }
+
+  int copy(bool back) {
+    auto cp = [&](void* dst, const void* src, size_t b) {
+      return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, s.stream);
+    };
+    cudaError_t e = cudaSuccess;
+    if (!back) {
+      if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
+      if (e == cudaSuccess && gb) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
+      if (e == cudaSuccess && s.rest[par]) e = cp(rs, s.rest[par], n * 4);
+      for (int i = 0; i < s.nphi(); ++i)
+        if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + i * n * 4, s.p[i], n * 4);
+      if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
+    } else {
+      if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
+      if (e == cudaSuccess && gb) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
+      if (e == cudaSuccess && s.rest[par]) e = cp(s.rest[par], rs, n * 4);
+      for (int i = 0; i < s.nphi(); ++i)
+        if (e == cudaSuccess) e = cp(s.p[i], static_cast<char*>(ps) + i * n * 4, n * 4);
+      if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);
+      // Reference-mode shells keep f = W_l in both buffers; the other buffer's interior
+      // is rewritten by the next update.
+      if (e == cudaSuccess) e = cp(s.f[par ^ 1], fs, fb);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) return fail(MCB_ERR_CUDA, "autotune copy: %s", cudaGetErrorString(e));
+    return MCB_OK;
+  }
+
+  int take() {
+    par = s.parity;
+    n = static_cast<size_t>(s.cells_total);
+    eq = s.gmode == mcb::kGEquil;
+    fb = s.f_bytes();
+    // g state: stored populations, or with equilibrium g the (phi, J) records of the TMA
+    // variant (none in push mode).
+    gb = eq ? (s.jbuf ? n * sizeof(float4) : 0) : n * 18 * pop_bytes(s.storage);
+    if (cudaMalloc(&fs, fb) != cudaSuccess || (gb && cudaMalloc(&gs, gb) != cudaSuccess) ||
+        cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 16) != cudaSuccess ||
+        cudaMalloc(&ms, n * 20) != cudaSuccess)
+      return fail(MCB_ERR_ALLOC, "autotune: no room for a state copy");
+    first = s.first;
+    latest = s.latest_p;
+    pk = s.pk;
+    update = s.update;
+    return copy(false);
+  }
+
+  int restore() {
+    MCB_TRY(copy(true));
+    s.parity = par;
+    s.pk = pk;
+    s.first = first;
+    s.latest_p = latest;
+    s.update = update;
+    return MCB_OK;
+  }
+};
 
 struct mcb_handle {
   Solver s;
@@ -1146,7 +1314,7 @@ int mcb_checkpoint_load(mcb_handle* h, const char* path) {
 int mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk) {
   if (!h || !variant || !zchunk) return fail(MCB_ERR_INVALID, "NULL argument");
   *variant = h->s.variant;
-  *zchunk = h->s.zchunk;
+  *zchunk = h->s.groups.empty() ? h->s.zchunk_req : h->s.groups[0].zchunk;
   return MCB_OK;
 }
 
@@ -1192,98 +1360,32 @@ int mcb_autotune(mcb_handle* h, int nsteps, int* best_variant, int* best_zchunk,
   Solver& s = h->s;
   if (!s.fields_set[0]) return fail(MCB_ERR_STATE, "fields are not set");
   MCB_TRY(s.set_device());
-  // Save the state the next update reads, so every trial starts from it.
-  const int par = s.parity;
-  const size_t n = static_cast<size_t>(s.cells_total);
-  const bool eq = s.gmode == mcb::kGEquil;
-  const size_t fb = s.f_bytes();
-  // g state: stored populations, or with equilibrium g the (phi, J) records of the TMA
-  // variant (none in push mode).
-  const size_t gb = eq ? (s.jbuf ? n * sizeof(float4) : 0) : n * 18 * pop_bytes(s.storage);
-  void *fs = nullptr, *gs = nullptr, *rs = nullptr, *ps = nullptr, *ms = nullptr;
-  auto free_all = [&]() {
-    cudaFree(fs);
-    cudaFree(gs);
-    cudaFree(rs);
-    cudaFree(ps);
-    cudaFree(ms);
-  };
-  if (cudaMalloc(&fs, fb) != cudaSuccess || (gb && cudaMalloc(&gs, gb) != cudaSuccess) ||
-      cudaMalloc(&rs, n * 4) != cudaSuccess || cudaMalloc(&ps, n * 16) != cudaSuccess ||
-      cudaMalloc(&ms, n * 20) != cudaSuccess) {
-    free_all();
-    return fail(MCB_ERR_ALLOC, "autotune: no room for a state copy");
-  }
-  const int save_first = s.first, save_latest = s.latest_p, save_variant = s.variant;
-  const int save_pk = s.pk;
-  const int save_zreq = s.zchunk_req;
-  const long long save_update = s.update;
-  auto snapshot = [&](bool restore) -> int {
-    auto cp = [&](void* dst, const void* src, size_t b) {
-      return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, s.stream);
-    };
-    cudaError_t e = cudaSuccess;
-    if (!restore) {
-      if (e == cudaSuccess) e = cp(fs, s.f[par], fb);
-      if (e == cudaSuccess && gb) e = cp(gs, eq ? s.jbuf : s.g[par], gb);
-      if (e == cudaSuccess && s.rest[par]) e = cp(rs, s.rest[par], n * 4);
-      for (int i = 0; i < s.nphi(); ++i)
-        if (e == cudaSuccess) e = cp(static_cast<char*>(ps) + i * n * 4, s.p[i], n * 4);
-      if (e == cudaSuccess) e = cp(ms, s.macros, n * 20);
-    } else {
-      if (e == cudaSuccess) e = cp(s.f[par], fs, fb);
-      if (e == cudaSuccess && gb) e = cp(eq ? s.jbuf : s.g[par], gs, gb);
-      if (e == cudaSuccess && s.rest[par]) e = cp(s.rest[par], rs, n * 4);
-      for (int i = 0; i < s.nphi(); ++i)
-        if (e == cudaSuccess) e = cp(s.p[i], static_cast<char*>(ps) + i * n * 4, n * 4);
-      if (e == cudaSuccess) e = cp(s.macros, ms, n * 20);
-      // Reference-mode shells keep f = W_l in both buffers; the other buffer's interior
-      // is rewritten by the next update.
-      if (e == cudaSuccess) e = cp(s.f[par ^ 1], fs, fb);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
-    if (e != cudaSuccess) return fail(MCB_ERR_CUDA, "autotune copy: %s", cudaGetErrorString(e));
-    s.parity = par;
-    s.pk = save_pk;
-    s.first = save_first;
-    s.latest_p = save_latest;
-    s.update = save_update;
-    return MCB_OK;
-  };
-  int rc = snapshot(false);
+  StateCopy snap(s);
+  int rc = snap.take();
+  const int save_variant = s.variant, save_zreq = s.zchunk_req;
   double best = -1.0;
-  int bv = save_variant, bz = s.zchunk;
+  int bv = save_variant, bz = s.zchunk_req;
   // The default split, balanced ranges of 1..4 resident waves, then fixed chunks.
   const int zc_list[] = {0, -1, -2, -3, -4, 8, 16, 32};
   for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
-    // The f layout is fixed at creation: the TMA variant alone on the padded layout, the
-    // plain tiles otherwise.
-    if ((v == mcb::kTmaVariant) != s.padded) continue;
-    if ((s.qf == 27 || s.ratio) && v != 0) continue;  // these run the 32x8 tile
-    if (v == mcb::kPairVariant && !s.pair_ok) continue;
-    if (s.wide_blocked && v != mcb::kPairVariant) continue;
+    if (!s.variant_fits(v)) continue;
     for (int zc : zc_list) {
       if (zc > s.cfg[0].nz) continue;
       s.variant = v;
       s.zchunk_req = zc;
+      double mlups = 0.0;
       rc = s.build_tiles();
+      if (rc == MCB_OK) rc = s.time_updates(nsteps, &mlups);
       if (rc != MCB_OK) break;
-      rc = s.step(2);  // warm-up (also takes the graph capture out of the timing)
-      if (rc == MCB_OK) rc = s.step(nsteps);
-      float ms = 0.f;
-      if (rc == MCB_OK) rc = s.last_ms(&ms);
-      if (rc != MCB_OK) break;
-      const double mlups = static_cast<double>(s.cells_total) * nsteps / (ms * 1e-3) / 1e6;
       if (mlups > best) {
         best = mlups;
         bv = v;
         bz = zc;
       }
-      rc = snapshot(true);
+      rc = snap.restore();
       if (rc != MCB_OK) break;
     }
   }
-  free_all();
   s.variant = (rc == MCB_OK) ? bv : save_variant;
   s.zchunk_req = (rc == MCB_OK) ? bz : save_zreq;
   const int rb = s.build_tiles();
@@ -1344,6 +1446,137 @@ int mcb_batch_diagnostics(mcb_batch* b, int ci, mcb_diag* out) {
 int mcb_batch_last_step_ms(mcb_batch* b, float* ms) {
   if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
   return b->s.last_ms(ms);
+}
+
+int mcb_batch_get_schedule(const mcb_batch* b, int case_index, int* variant, int* zchunk) {
+  if (!b || !variant || !zchunk) return fail(MCB_ERR_INVALID, "NULL argument");
+  if (case_index < 0 || case_index >= static_cast<int>(b->s.cases.size()))
+    return fail(MCB_ERR_INVALID, "case index %d out of range", case_index);
+  b->s.schedule_of(case_index, variant, zchunk);
+  return MCB_OK;
+}
+
+int mcb_batch_autotune(mcb_batch* b, int nsteps, double* default_mlups, double* tuned_mlups) {
+  if (!b) return fail(MCB_ERR_INVALID, "batch is NULL");
+  if (nsteps < 2) return fail(MCB_ERR_INVALID, "nsteps must be >= 2");
+  Solver& s = b->s;
+  for (size_t i = 0; i < s.fields_set.size(); ++i)
+    if (!s.fields_set[i]) return fail(MCB_ERR_STATE, "fields of case %zu are not set", i);
+  MCB_TRY(s.set_device());
+  using Group = Solver::Group;
+  StateCopy snap(s);
+  MCB_TRY(snap.take());
+  // The untuned schedule: one launch of every case with the batch's variant and split.
+  const std::vector<Group> before = s.groups;
+  const bool before_grouped = s.grouped;
+  s.grouped = false;
+  double base = 0.0;
+  int rc = s.build_tiles();
+  if (rc == MCB_OK) rc = s.time_updates(nsteps, &base);
+  if (rc == MCB_OK) rc = snap.restore();
+  // Size classes: the cases of one lattice size.
+  std::vector<std::vector<int>> classes;
+  std::vector<std::array<int, 3>> keys;
+  for (int i = 0; i < static_cast<int>(s.cases.size()); ++i) {
+    const std::array<int, 3> k{s.cases[i].nx, s.cases[i].ny, s.cases[i].nz};
+    size_t c = 0;
+    while (c < keys.size() && keys[c] != k) ++c;
+    if (c == keys.size()) {
+      keys.push_back(k);
+      classes.emplace_back();
+    }
+    classes[c].push_back(i);
+  }
+  // Each class alone: every variant that fits, with the group's default split or a fixed
+  // chunk (fixed chunks can differ per case inside one launch; balanced runs cannot).
+  const int zc_list[] = {0, 8, 16, 24, 32, 48, 64};
+  std::vector<int> best_v(classes.size(), s.variant), best_z(classes.size(), 0);
+  for (size_t c = 0; c < classes.size() && rc == MCB_OK; ++c) {
+    double best = -1.0;
+    for (int v = 0; v < mcb::kNumVariants && rc == MCB_OK; ++v) {
+      if (!s.variant_fits(v)) continue;
+      for (int zc : zc_list) {
+        if (zc > keys[c][2]) continue;
+        Group g;
+        g.variant = v;
+        g.zchunk_req = zc;
+        g.members = classes[c];
+        s.groups.assign(1, g);
+        s.grouped = true;
+        double m = 0.0;
+        rc = s.build_tiles();
+        if (rc == MCB_OK) rc = s.time_updates(nsteps, &m);
+        if (rc == MCB_OK) rc = snap.restore();
+        if (rc != MCB_OK) break;
+        if (m > best) {
+          best = m;
+          best_v[c] = v;
+          best_z[c] = zc;
+        }
+      }
+    }
+  }
+  // Two ways to combine the choices: one launch per chosen variant, each case with its
+  // class's chunk; or one launch of every case with the variant that covers the most cells.
+  std::vector<std::vector<Group>> plans;
+  if (rc == MCB_OK) {
+    std::vector<Group> per_variant;
+    std::vector<long long> cells_of(mcb::kNumVariants, 0);
+    for (size_t c = 0; c < classes.size(); ++c) {
+      size_t gi = 0;
+      while (gi < per_variant.size() && per_variant[gi].variant != best_v[c]) ++gi;
+      if (gi == per_variant.size()) {
+        per_variant.emplace_back();
+        per_variant.back().variant = best_v[c];
+      }
+      for (int ci : classes[c]) {
+        per_variant[gi].members.push_back(ci);
+        per_variant[gi].zc_case.push_back(best_z[c]);
+        cells_of[best_v[c]] += s.cases[ci].ncell;
+      }
+    }
+    plans.push_back(per_variant);
+    if (per_variant.size() > 1) {
+      Group one;
+      one.variant = static_cast<int>(
+          std::max_element(cells_of.begin(), cells_of.end()) - cells_of.begin());
+      for (size_t c = 0; c < classes.size(); ++c)
+        for (int ci : classes[c]) {
+          one.members.push_back(ci);
+          one.zc_case.push_back(best_z[c]);
+        }
+      plans.push_back({one});
+    }
+  }
+  double tuned = base;
+  std::vector<Group> chosen;
+  for (const auto& plan : plans) {
+    if (rc != MCB_OK) break;
+    s.groups = plan;
+    s.grouped = true;
+    double m = 0.0;
+    rc = s.build_tiles();
+    if (rc == MCB_OK) rc = s.time_updates(nsteps, &m);
+    if (rc == MCB_OK) rc = snap.restore();
+    if (rc == MCB_OK && m > tuned) {
+      tuned = m;
+      chosen = plan;
+    }
+  }
+  // Keep the fastest measured schedule; the untuned one if nothing beat it.
+  if (rc == MCB_OK) {
+    s.grouped = !chosen.empty();
+    if (s.grouped) s.groups = chosen;
+  } else {
+    s.grouped = before_grouped;
+    s.groups = before;
+  }
+  const int rb = s.build_tiles();
+  if (rc != MCB_OK) return rc;
+  if (rb != MCB_OK) return rb;
+  if (default_mlups) *default_mlups = base;
+  if (tuned_mlups) *tuned_mlups = tuned;
+  return MCB_OK;
 }
 
 int mcb_batch_cells(const mcb_batch* b, int64_t* cells) {

@@ -1454,6 +1454,9 @@ const void* phi_kernel(int variant, bool eq, dim3* block) {
   switch (variant) {
     case 0:
     case kPairVariant:
+    case kPairVariant + 1:
+    case kPairVariant + 2:
+    case kPairVariant + 3:
     case kTmaVariant: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
     case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
     case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
@@ -1470,10 +1473,14 @@ const void* collide_kernel(int variant, dim3* block) {
     case 2: *block = dim3(64, 4); return reinterpret_cast<const void*>(k_collide<S, GM, 64, 4>);
     case 3: *block = dim3(16, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 8>);
     case kPairVariant:
-      // two cells per thread: equilibrium g only
+    case kPairVariant + 1:
+    case kPairVariant + 2:
+    case kPairVariant + 3:
+      // two cells per thread: equilibrium g only (the instance with the reference-mode
+      // shell, which runs every mode; launches pick by StepArgs::has_ref)
       if constexpr (GM == kGEquil) {
         *block = dim3(kPairTX, kPairBY);
-        return reinterpret_cast<const void*>(k_collide_pair<S, kPairBY>);
+        return pair_kernel<S>(variant, false);
       } else {
         return nullptr;
       }
@@ -1546,7 +1553,7 @@ cudaError_t prepare_tma_kernel() {
 template <class S>
 cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int wide, int* phi_blocks,
                          int* collide_blocks) {
-  if (variant != kPairVariant && (qf == kQ27 || ratio || wide)) {
+  if (!is_pair_variant(variant) && (qf == kQ27 || ratio || wide)) {
     dim3 bp;
     const void* fp = phi_kernel<S>(0, gmode == kGEquil, &bp);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -1597,7 +1604,11 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
                                       const void* tmap, cudaStream_t s) {                  \
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
-    if (variant != kPairVariant && (a.qf == kQ27 || a.ratio || a.wide))                    \
+    if (is_pair_variant(variant))                                                          \
+      return gmode == kGEquil ? launch_on(pair_kernel<S>(variant, a.has_ref != 0),          \
+                                          a.grid_collide, dim3(kPairTX, kPairBY), a, s)     \
+                              : cudaErrorInvalidValue;                                     \
+    if (a.qf == kQ27 || a.ratio || a.wide)                                                 \
       return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0, a.wide != 0),        \
                        a.grid_collide, dim3(32, 8), a, s);                                 \
     dim3 block;                                                                            \

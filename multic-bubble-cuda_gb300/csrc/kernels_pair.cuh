@@ -87,7 +87,9 @@ namespace {
 
 constexpr int kPairTX = 32;  // threads in x; a tile is 2 * kPairTX = 64 cells wide
 
-template <class S, int BY>
+// kRef: some case of the launch is in reference mode (frozen shell); the shell handling is
+// compiled only into that instance, which also runs the other modes.
+template <class S, int BY, bool kAhead, bool kRef>
 __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Tile& t) {
   using FT = typename S::FT;
   using IO = pk::PairIO<S>;
@@ -112,7 +114,8 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
 
   const int nx = t.nx, ny = t.ny, nz = t.nz;
   const int nxy = nx * ny;
-  const bool ref = t.bc == kBcRef, walls = t.bc == kBcWallsZ;
+  const bool ref = kRef && t.bc == kBcRef;
+  const bool walls = t.bc == kBcWallsZ;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
   const int x0 = t.xt + 2 * tx, y = t.yt + ty;
   const bool active = x0 < nx && y < ny;  // nx is even: x0 + 1 < nx with x0
@@ -261,6 +264,38 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
 
   // Two cells' worth of one population: the gathered pair (values of x0, x0 + 1).
   float2 fr[QF];
+  // Gathers the 19 populations of both cells of plane z and their Q2.30 phi.
+  auto gather = [&](int z, int2& pcv) {
+    const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
+    pcv = __ldg(reinterpret_cast<const int2*>(pcur + x0 + yo + z * nxy));
+    const FT* pz0 = fin + static_cast<long long>(z) * PS;
+    const FT* pzm = fin + static_cast<long long>(z == 0 ? nz - 1 : z - 1) * PS;
+    const FT* pzp = fin + static_cast<long long>(z == nz - 1 ? 0 : z + 1) * PS;
+    auto pull = [&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      const FT* row = src_of<cz(L)>(pzm, pz0, pzp) + src_of<cy(L)>(fym, fy0, fyp) + L * 32;
+      if constexpr (cx(L) == 0) {
+        fr[L] = IO::ld2(row + fx0);
+      } else if constexpr (cx(L) == 1) {  // sources x0 - 1 and x0
+        fr[L] = make_float2(IO::ld1(row + fxm), IO::ld1(row + fx0));
+      } else {  // sources x0 + 1 and x0 + 2
+        fr[L] = make_float2(IO::ld1(row + fx0 + 1), IO::ld1(row + fxp));
+      }
+    };
+    fr[0] = IO::ld2(pz0 + fy0 + fx0);
+    if (blo || bhi) {
+      // A wall plane: what left through the wall returns as the cell's own opposite
+      // population.
+      static_for<1, QF>([&](auto LC) {
+        constexpr int L = decltype(LC)::value;
+        const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+        if (bounce) fr[L] = IO::ld2(pz0 + fy0 + fx0 + opp(L) * 32);
+        else pull(LC);
+      });
+    } else {
+      static_for<1, QF>(pull);
+    }
+  };
 
   // Prologue: phi planes zb-2 .. zb+2, normals zb-1 .. zb+1.
   for (int zpl = t.zb - 2; zpl <= t.zb + 2; ++zpl) {
@@ -268,6 +303,11 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     commit(zpl);
   }
   issue(t.zb + 3);
+  int2 pc = make_int2(0, 0), pcn = pc;
+  // kAhead: the populations of a plane are gathered one plane early, right after the
+  // previous plane's moments, so their latency overlaps that plane's collision, push and
+  // barrier as well as the normals.
+  if (kAhead && active) gather(t.zb, pcn);
   __syncthreads();
   for (int zpl = t.zb - 1; zpl <= t.zb + 1; ++zpl) normals(zpl);
   __syncthreads();
@@ -279,42 +319,12 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     const int idx = x0 + yo + z * nxy;
     const bool zshell = ref && (z == 0 || z == nz - 1);
     const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
-    int2 pc = make_int2(0, 0);
-    if (active) {
-      pc = __ldg(reinterpret_cast<const int2*>(pcur + idx));
-      // Pull the 19 populations of both cells.
-      const FT* pz0 = fin + static_cast<long long>(z) * PS;
-      const FT* pzm = fin + static_cast<long long>(z == 0 ? nz - 1 : z - 1) * PS;
-      const FT* pzp = fin + static_cast<long long>(z == nz - 1 ? 0 : z + 1) * PS;
-      auto pull = [&](auto LC) {
-        constexpr int L = decltype(LC)::value;
-        const FT* row = src_of<cz(L)>(pzm, pz0, pzp) + src_of<cy(L)>(fym, fy0, fyp) + L * 32;
-        if constexpr (cx(L) == 0) {
-          fr[L] = IO::ld2(row + fx0);
-        } else if constexpr (cx(L) == 1) {  // sources x0 - 1 and x0
-          fr[L] = make_float2(IO::ld1(row + fxm), IO::ld1(row + fx0));
-        } else {  // sources x0 + 1 and x0 + 2
-          fr[L] = make_float2(IO::ld1(row + fx0 + 1), IO::ld1(row + fxp));
-        }
-      };
-      fr[0] = IO::ld2(pz0 + fy0 + fx0);
-      if (blo || bhi) {
-        // A wall plane: what left through the wall returns as the cell's own opposite
-        // population.
-        static_for<1, QF>([&](auto LC) {
-          constexpr int L = decltype(LC)::value;
-          const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
-          if (bounce) fr[L] = IO::ld2(pz0 + fy0 + fx0 + opp(L) * 32);
-          else pull(LC);
-        });
-      } else {
-        static_for<1, QF>(pull);
-      }
-    }
+    if (!kAhead && active) gather(z, pcn);
     __syncthreads();
     if (z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
     if (z + 2 <= t.ze) normals(z + 2);
     if (!active) continue;
+    pc = pcn;
 
     *reinterpret_cast<int2*>(pzero + idx) = make_int2(0, 0);  // next update accumulates here
     // Reference-mode shell cells of this pair (never collide; rest-equilibrium inflow).
@@ -369,6 +379,7 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
       if constexpr (cx(L) * cz(L) != 0) sxz = pk::addsg<cx(L) * cz(L)>(sxz, sp);
       if constexpr (cy(L) * cz(L) != 0) syz = pk::addsg<cy(L) * cz(L)>(syz, sp);
     });
+    if (kAhead && z + 1 < t.ze) gather(z + 1, pcn);
     const float2 inv_rho = make_float2(__frcp_rn(rho.x), __frcp_rn(rho.y));
     const float2 ux = mul(fma(dup(0.5f), Fx, jx), inv_rho);
     const float2 uy = mul(fma(dup(0.5f), Fy, jy), inv_rho);
@@ -398,7 +409,7 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     FT* __restrict__ fo_base = fout + static_cast<long long>(z) * PS + fy0 + fx0;
     // The shell lanes keep the value the init wrote: f = W (0 in deviation form).
     auto put = [&](int L, float2 v) {
-      if (sh0 || sh1) {
+      if (kRef && (sh0 || sh1)) {
         const float wv = kDevF ? 0.0f : wf(L);
         if (sh0) v.x = wv;
         if (sh1) v.y = wv;
@@ -437,10 +448,12 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     const float2 Jy = scale(fma(phi3, uy, mul(A, ncy)), kj);
     const float2 Jz = scale(fma(phi3, uz, mul(A, ncz)), kj);
     // shell lanes push their phi with no flux
-    const JQ j0 = sh0 ? JQ{0, 0, 0}
-                      : JQ{__float2int_rn(Jx.x), __float2int_rn(Jy.x), __float2int_rn(Jz.x)};
-    const JQ j1 = sh1 ? JQ{0, 0, 0}
-                      : JQ{__float2int_rn(Jx.y), __float2int_rn(Jy.y), __float2int_rn(Jz.y)};
+    JQ j0{__float2int_rn(Jx.x), __float2int_rn(Jy.x), __float2int_rn(Jz.x)};
+    JQ j1{__float2int_rn(Jx.y), __float2int_rn(Jy.y), __float2int_rn(Jz.y)};
+    if (kRef) {
+      if (sh0) j0 = JQ{0, 0, 0};
+      if (sh1) j1 = JQ{0, 0, 0};
+    }
     {
       const int wf0 = wsplit_face(pc.x), we0 = wsplit_edge_of_face(wf0);
       const int wf1 = wsplit_face(pc.y), we1 = wsplit_edge_of_face(wf1);
@@ -506,7 +519,7 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
         });
       }
     }
-    if (sh0 || sh1) {
+    if (kRef && (sh0 || sh1)) {
       // The shell's own next phi is the lagged copy of its nearest interior cell
       // (boundaryConditions, src/lbm.cu:403-425).
       const int zc = clampi(z, 1, nz - 2) * nxy, yc = clampi(y, 1, ny - 2) * nx;
@@ -517,8 +530,8 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     if (a.macros) {
       const long long T = a.cells_total, o = t.cell_off + idx;
       float2 mphi = phi, mrho = rho, mx = ux, my = uy, mz = uz;
-      if (sh0) { mphi.x = __int2float_rn(pc.x) * kInvQ30; mrho.x = 1.f; mx.x = my.x = mz.x = 0.f; }
-      if (sh1) { mphi.y = __int2float_rn(pc.y) * kInvQ30; mrho.y = 1.f; mx.y = my.y = mz.y = 0.f; }
+      if (kRef && sh0) { mphi.x = __int2float_rn(pc.x) * kInvQ30; mrho.x = 1.f; mx.x = my.x = mz.x = 0.f; }
+      if (kRef && sh1) { mphi.y = __int2float_rn(pc.y) * kInvQ30; mrho.y = 1.f; mx.y = my.y = mz.y = 0.f; }
       *reinterpret_cast<float2*>(a.macros + o) = mphi;
       *reinterpret_cast<float2*>(a.macros + T + o) = mrho;
       *reinterpret_cast<float2*>(a.macros + 2 * T + o) = mx;
@@ -534,11 +547,26 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
 // Resident warps per SM of the pair kernel: four blocks of four warps (128 registers).
 constexpr int kPairWarpsPerSM = 16;
 
-template <class S, int BY>
-__global__ void __launch_bounds__(kPairTX * BY, kPairWarpsPerSM * 32 / (kPairTX * BY))
+template <class S, int BY, bool kAhead, bool kRef, int kMinBlocks>
+__global__ void __launch_bounds__(kPairTX * BY, kMinBlocks)
     k_collide_pair(const StepArgs a) {
   for_each_segment<2 * kPairTX, BY, true>(
-      a, [&](const Tile& t) { collide_pair_segment<S, BY>(a, t); }, a.balanced != 0);
+      a, [&](const Tile& t) { collide_pair_segment<S, BY, kAhead, kRef>(a, t); },
+      a.balanced != 0);
+}
+
+// The pair kernel of a tile variant, with or without the reference-mode shell handling.
+template <class S>
+const void* pair_kernel(int variant, bool with_ref) {
+  constexpr int B = kPairWarpsPerSM * 32 / (kPairTX * kPairBY);
+  if (variant == kPairVariant || with_ref)
+    return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, true, B>)
+                    : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, false, B>);
+  switch (variant) {
+    case kPairVariant + 1: return reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, false, 5>);
+    case kPairVariant + 2: return reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, false, 3>);
+    default: return reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, false, 3>);
+  }
 }
 
 }  // namespace

@@ -37,7 +37,7 @@ EXPORTS = [
     "mcb_batch_set_fields", "mcb_batch_step", "mcb_batch_get_field", "mcb_batch_diagnostics",
     "mcb_batch_last_step_ms", "mcb_batch_cells", "mcb_diagnostics_device",
     "mcb_checkpoint_save", "mcb_checkpoint_load", "mcb_dump_field", "mcb_get_schedule",
-    "mcb_get_phi_q30",
+    "mcb_get_phi_q30", "mcb_batch_autotune", "mcb_batch_get_schedule",
 ]
 
 
@@ -130,6 +130,8 @@ def lib() -> C.CDLL:
             "mcb_batch_diagnostics": [vp, C.c_int, C.POINTER(Diag)],
             "mcb_batch_last_step_ms": [vp, _FP],
             "mcb_batch_cells": [vp, C.POINTER(C.c_int64)],
+            "mcb_batch_autotune": [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+            "mcb_batch_get_schedule": [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)],
             "mcb_diagnostics_device": [vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
                                        C.c_int, vp, C.POINTER(Diag)],
         }
@@ -402,3 +404,15 @@ class Batch:
         c = C.c_int64()
         _check(lib().mcb_batch_cells(self._h, C.byref(c)))
         return c.value
+
+    def autotune(self, nsteps: int = 20) -> tuple[float, float]:
+        """Per-size-class tile choice (mcb_batch_autotune): (untuned, tuned) MLUPS."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().mcb_batch_autotune(self._h, nsteps, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def schedule(self, i) -> tuple[int, int]:
+        """(tile variant, z chunk setting) case i runs."""
+        v, z = C.c_int(), C.c_int()
+        _check(lib().mcb_batch_get_schedule(self._h, i, C.byref(v), C.byref(z)))
+        return v.value, z.value
