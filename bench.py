@@ -216,9 +216,18 @@ def pinned_like(a):
     return t, v
 
 
+PAIR_VARIANTS = (5, 6)  # the two-cells-per-thread collide (k_collide_pair)
+KERNEL_OF = {}  # (storage, tau_g) -> name of the collide kernel the device leg ran
+
+
+def collide_name(variant: int) -> str:
+    return "k_collide_pair" if variant in PAIR_VARIANTS else "k_collide"
+
+
 def device_run(storage, device, steps, warmup, dist, tau_g=None):
     """Device-resident timing: K updates, an event after every kernel."""
     s, cfg, fields = make_solver(storage, device, tau_g)
+    KERNEL_OF[(storage, tau_g)] = collide_name(s.schedule[0])
     s.set_fields(*fields)
     s.step(warmup)
     s.synchronize()
@@ -295,6 +304,7 @@ def storage_leg(device, steps, warmup, storage, tau_g=None):
     _, col_b, upd_b = bytes_per_lu(cfg, storage)
     col_s = t_col * 1e-3 / steps
     return {"storage": storage, "tau_g": cfg.tau_g, "g_storage": g_storage(cfg),
+            "kernel": KERNEL_OF[(storage, tau_g)],
             "value": cells * steps / (total * 1e-3) / 1e6, "unit": "MLUPS", "steps": steps,
             "kernel_ms": {"phi_stage": t_phi / steps, "k_collide": t_col / steps},
             "roofline": {"bytes_per_lu": col_b, "achieved": col_b * cells / col_s / 1e9,
@@ -430,6 +440,14 @@ def batch_run(device, steps, ncases=64):
         b.step(steps)
         ms_batch = b.last_step_ms()
         cells = b.cells
+        # per-size-class tile choice, then the same timing with the chosen schedule
+        at_default, at_tuned = b.autotune(nsteps=20)
+        b.step(warm)
+        b.step(steps)
+        ms_tuned = b.last_step_ms()
+        classes = {}
+        for i, c in enumerate(cfgs):
+            classes.setdefault(f"{c.nx}", list(b.schedule(i)))
     ms_seq = 0.0
     for c, (_, phi, *_r) in zip(cfgs, cases):
         with mcb.Solver(c) as s:
@@ -439,8 +457,11 @@ def batch_run(device, steps, ncases=64):
             ms_seq += s.last_step_ms()
     return {"cases": ncases, "cells": cells, "storage": "f16", "steps": steps,
             "batch_mlups": cells * steps / (ms_batch * 1e-3) / 1e6,
+            "batch_tuned_mlups": cells * steps / (ms_tuned * 1e-3) / 1e6,
+            "autotune_trials_mlups": {"default": at_default, "tuned": at_tuned},
+            "tuned_schedule_by_edge": classes,
             "sequential_mlups": cells * steps / (ms_seq * 1e-3) / 1e6,
-            "speedup": ms_seq / ms_batch}
+            "speedup": ms_seq / ms_batch, "speedup_tuned": ms_seq / ms_tuned}
 
 
 def d3q27_run(device, steps, storage="f32"):
@@ -636,7 +657,8 @@ def main():
                    "l2": f"inputs larger than L2 (f in and out: "
                          f"{2 * 19 * (4 if st == 'f32' else 2) * cells / 1e6:.0f} MB per update)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
-        "roofline": {"bound": "hbm", "kernel": "k_collide", "achieved": achieved, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": KERNEL_OF[(st, None)], "achieved": achieved,
+                     "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": f"{peak_kind} HBM copy bandwidth",
                      "bytes_per_lu": col_b, "g_storage": gs,

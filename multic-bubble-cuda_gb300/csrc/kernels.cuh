@@ -1455,8 +1455,6 @@ const void* phi_kernel(int variant, bool eq, dim3* block) {
     case 0:
     case kPairVariant:
     case kPairVariant + 1:
-    case kPairVariant + 2:
-    case kPairVariant + 3:
     case kTmaVariant: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
     case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
     case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
@@ -1474,8 +1472,6 @@ const void* collide_kernel(int variant, dim3* block) {
     case 3: *block = dim3(16, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 8>);
     case kPairVariant:
     case kPairVariant + 1:
-    case kPairVariant + 2:
-    case kPairVariant + 3:
       // two cells per thread: equilibrium g only (the instance with the reference-mode
       // shell, which runs every mode; launches pick by StepArgs::has_ref)
       if constexpr (GM == kGEquil) {

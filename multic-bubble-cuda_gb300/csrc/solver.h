@@ -128,19 +128,19 @@ struct DiagArgs {
   DiagPartial* result;    // one entry
 };
 
-constexpr int kNumVariants = 9;
+constexpr int kNumVariants = 7;
 struct Variant { int bx, by; };
 // Cell tiles of the variants. Variant 4 is the 32x8 collide that stages f through the tensor
 // memory accelerator (TMA) on the padded f layout; it needs one case, (phi, J) records and nx
 // a multiple of 16 bytes. Variants 5 and 6 take two neighbouring cells in x per thread (64x4
-// cells, 32x4 threads); they need equilibrium g, D3Q19 f at density ratio 1 and an even nx in
-// every case. Variant 6 gathers each plane's populations one plane ahead.
+// cells, 32x4 threads; three and two blocks per SM); they need equilibrium g, D3Q19 f at
+// density ratio 1 and an even nx in every case.
 constexpr Variant kVariants[kNumVariants] = {{32, 8}, {16, 16}, {64, 4}, {16, 8}, {32, 8},
-                                             {64, 4}, {64, 4}, {64, 4}, {64, 4}};
+                                             {64, 4}, {64, 4}};
 constexpr int kTmaVariant = 4;
 constexpr int kPairVariant = 5;
 constexpr int kPairBY = 4;  // thread rows of the pair kernel's block
-constexpr bool is_pair_variant(int v) { return v >= kPairVariant && v <= kPairVariant + 3; }
+constexpr bool is_pair_variant(int v) { return v == kPairVariant || v == kPairVariant + 1; }
 constexpr int kErrTmaWait = 1;  // StepArgs::err: a TMA wait timed out
 constexpr int kDiagBlocks = 304;   // fixed grid: the reduction order never changes
 constexpr int kDiagThreads = 256;

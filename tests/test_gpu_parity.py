@@ -230,13 +230,16 @@ def test_tma_collide_is_skipped_where_it_does_not_apply():
     cfg.variant = 4
     with mcb.Solver(cfg) as s:
         assert s.schedule[0] == 0
-    # the default is the plain tile
+    # the default is the two-cells-per-thread tile where it applies, else the 32x8 tile
     cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30))
+    with mcb.Solver(cfg) as s:
+        assert s.schedule[0] == PAIR
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30), tau_g=0.8)
     with mcb.Solver(cfg) as s:
         assert s.schedule[0] == 0
 
 
-PAIR = 5  # the two-cells-per-thread tile variants: 5, and 6 (gathers one plane ahead)
+PAIR = 5  # the two-cells-per-thread tile variants: 5 (three blocks per SM) and 6 (two)
 PAIRS = (5, 6)
 
 
