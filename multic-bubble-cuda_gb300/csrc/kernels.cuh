@@ -793,6 +793,44 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
   float4* __restrict__ jout = EQ ? static_cast<float4*>(a.j) + t.cell_off : nullptr;
   const int* __restrict__ pprev = a.p_prev + t.cell_off;
 
+  // 16-bit relaxed g decodes every pulled population against the weight split of its source
+  // cell's previous phi. A 4-plane ring of that previous phi (tile + halo 1, exact integers)
+  // serves the 18 sources of a cell from shared memory instead of 18 global loads. Plane q
+  // sits in slot q & 3; the slot of plane z + 2 is written after the barrier of plane z,
+  // when every thread has finished plane z - 1, the last to read plane z - 2 there.
+  // (Only where the block's static shared memory stays within 48 KB: not the 64x4 tile.)
+  constexpr int kSmemNoRing = (5 * PP + 16 * HP + 4 * HP + HP) * 4;
+  constexpr bool kPRing = BGK && S::kDev && !kTma && kSmemNoRing + 16 * HP <= 48 * 1024;
+  constexpr int KPR = kPRing ? (HP + NT - 1) / NT : 1;
+  __shared__ int sprev[kPRing ? 4 : 1][kPRing ? HP : 1];
+  int proff[KPR], ppre[KPR];
+  if constexpr (kPRing) {
+#pragma unroll
+    for (int k = 0; k < KPR; ++k) {
+      const int i = tid + k * NT;
+      int gx = t.xt - 1 + i % HX, gy = t.yt - 1 + i / HX;  // reference mode has no BGK g
+      gx = ((gx % nx) + nx) % nx;
+      gy = ((gy % ny) + ny) % ny;
+      proff[k] = i < HP ? gx + gy * nx : 0;
+    }
+  }
+  auto prev_issue = [&](int q) {
+    if constexpr (kPRing) {
+      const int zq = t.bc == kBcPeriodic ? wrap1(q, nz) : clampi(q, 0, nz - 1);
+      const int* base = pprev + static_cast<long long>(zq) * nxy;
+#pragma unroll
+      for (int k = 0; k < KPR; ++k)
+        if ((k + 1) * NT <= HP || tid + k * NT < HP) ppre[k] = __ldg(base + proff[k]);
+    }
+  };
+  auto prev_commit = [&](int q) {
+    if constexpr (kPRing) {
+#pragma unroll
+      for (int k = 0; k < KPR; ++k)
+        if ((k + 1) * NT <= HP || tid + k * NT < HP) sprev[q & 3][tid + k * NT] = ppre[k];
+    }
+  };
+
   // f layout of the stores: plain (fn = n, cell index) or padded (TMA variant).
   const long long fn = kTma ? t.fn : n;
   const bool ghosts = kTma && !ref;
@@ -863,6 +901,11 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
     commit(zpl);
   }
   issue(t.zb + 3);
+  for (int q = t.zb - 1; q <= t.zb + 1; ++q) {
+    prev_issue(q);
+    prev_commit(q);
+  }
+  prev_issue(t.zb + 2);
   __syncthreads();
   for (int zpl = t.zb - 1; zpl <= t.zb + 1; ++zpl) normals(zpl);
   __syncthreads();
@@ -958,6 +1001,10 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
       }
     }
     if constexpr (!kTma) __syncthreads();  // the TMA path synchronised in its wait
+    if constexpr (kPRing) {
+      prev_commit(z + 2);
+      if (z + 3 <= t.ze + 1) prev_issue(z + 3);
+    }
     if (kPush && z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
     if (z + 2 <= t.ze) normals(z + 2);
     if (!active) continue;
@@ -1192,7 +1239,10 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
 
     if constexpr (BGK) {
       // Incoming g (pull), decoded, then relaxed towards geq.
-      const int pself = S::kDev ? __ldg(pprev + idx) : 0;
+      const int hcp = (ty + 1) * HX + tx + 1;  // this cell in the previous-phi ring
+      int pself = 0;
+      if constexpr (kPRing) pself = sprev[z & 3][hcp];
+      else if constexpr (S::kDev) pself = __ldg(pprev + idx);
       static_for<1, kQ>([&](auto LC) {
         constexpr int L = decltype(LC)::value;
         constexpr int O = opp(L);
@@ -1203,7 +1253,9 @@ __device__ __forceinline__ void collide_segment(const StepArgs& a, const Tile& t
         } else {
           const int s = src_of<cz(L)>(zm, zo, zp) + src_of<cy(L)>(ym, yo, yp) +
                         src_of<cx(L)>(xm, x, xp);
-          const int ps = S::kDev ? __ldg(pprev + s) : 0;
+          int ps = 0;  // the source x - c_l: plane z - cz, row ty - cy, column tx - cx
+          if constexpr (kPRing) ps = sprev[(z - cz(L)) & 3][hcp - cy(L) * HX - cx(L)];
+          else if constexpr (S::kDev) ps = __ldg(pprev + s);
           gi = S::template g_dec<L>(S::gload(gin + (L - 1) * ng + s), ps);
         }
         const float gf = __int2float_rn(gi) * kInvQ30;

@@ -642,15 +642,15 @@ __global__ void __launch_bounds__(kPairTX * BY, kMinBlocks)
 
 // The pair kernel of a tile variant, with or without the reference-mode shell handling.
 // Variant 5: three blocks of four warps per SM (168 registers: no spills, and more
-// independent work per warp than four blocks at 128 registers, which measured 2 % slower at
-// FP16 storage and 10 % slower at FP32). Variant 6: two blocks per SM.
+// independent work per warp; two blocks per SM measured 12 % slower at FP16 storage and 26 %
+// at FP32). Variant 6: four blocks per SM (128 registers).
 template <class S>
 const void* pair_kernel(int variant, bool with_ref) {
   if (variant == kPairVariant)
     return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3>)
                     : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3>);
-  return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 2>)
-                  : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 2>);
+  return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 4>)
+                  : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 4>);
 }
 
 }  // namespace

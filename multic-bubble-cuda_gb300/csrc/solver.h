@@ -133,7 +133,7 @@ struct Variant { int bx, by; };
 // Cell tiles of the variants. Variant 4 is the 32x8 collide that stages f through the tensor
 // memory accelerator (TMA) on the padded f layout; it needs one case, (phi, J) records and nx
 // a multiple of 16 bytes. Variants 5 and 6 take two neighbouring cells in x per thread (64x4
-// cells, 32x4 threads; three and two blocks per SM); they need equilibrium g, D3Q19 f at
+// cells, 32x4 threads; three and four blocks per SM); they need equilibrium g, D3Q19 f at
 // density ratio 1 and an even nx in every case.
 constexpr Variant kVariants[kNumVariants] = {{32, 8}, {16, 16}, {64, 4}, {16, 8}, {32, 8},
                                              {64, 4}, {64, 4}};

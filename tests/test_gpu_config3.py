@@ -81,6 +81,7 @@ def test_config3_crop_rerun_against_the_oracle():
 
     def errs(a, b):
         return {"max_phi_err": float(np.max(np.abs(a["phi"] - b["phi"]))),
+                "rms_phi_err": float(np.sqrt(np.mean((a["phi"] - b["phi"]) ** 2))),
                 "max_u_err": float(max(np.max(np.abs(a[k] - b[k])) for k in ("ux", "uy", "uz"))),
                 "max_p_err": float(np.max(np.abs(a["p"] - b["p"])))}
 
@@ -109,9 +110,11 @@ def test_config3_crop_rerun_against_the_oracle():
             assert report[f"{name}@{h}"]["mass_drift_q30"] == 0, (name, h)
     # This multi-bubble flow amplifies rounding: the FP32 oracle, a faithful FP32 restatement,
     # parts from the FP64 one by 6.5e-4 in phi after 200 updates and 8.5e-3 after 5000
-    # (measured). Each storage is bounded against that floor at both horizons. Measured
-    # ratios: FP32 1.1 and 1.0, FP16 2.3 and 2.9, BF16 5.8 and 11.2.
-    mult = {"f32": 1.5, "f16": 4.0, "bf16": 15.0}
+    # (measured). Each storage is bounded against that floor at both horizons. The ratios
+    # move with FP32-level changes of the arithmetic (the one-cell and the two-cell collide,
+    # measured in phi at 200 and 5000 updates): FP32 1.1 and 1.0, or 0.3 and 0.5; FP16 2.3
+    # and 2.9, or 3.9 and 7.0; BF16 5.8 and 11.2, or 7.4 and 15.2.
+    mult = {"f32": 1.5, "f16": 10.0, "bf16": 25.0}
     for name, m in mult.items():
         for h in horizons:
             floor = report[f"oracle_f32@{h}"]

@@ -239,7 +239,7 @@ def test_tma_collide_is_skipped_where_it_does_not_apply():
         assert s.schedule[0] == 0
 
 
-PAIR = 5  # the two-cells-per-thread tile variants: 5 (three blocks per SM) and 6 (two)
+PAIR = 5  # the two-cells-per-thread tile variants: 5 (three blocks per SM) and 6 (four)
 PAIRS = (5, 6)
 
 
@@ -487,12 +487,21 @@ def test_autotune_restores_the_state(tau_g, storage):
     with mcb.Solver(cfg) as s:
         s.set_fields(phi, *u)
         s.step(10)
+        before = {k: s.get(k) for k in FIELDS}
+        v0 = s.schedule[0]
         v, zc, ml = s.autotune(nsteps=4)
         # zc > 0: fixed chunks; zc < 0: balanced over -zc waves; 0: the default split.
         assert 0 <= v < mcb.lib().mcb_variant_count() and -16 <= zc <= 64 and ml > 0
+        assert s.schedule[0] == v
+        for k in FIELDS:  # the trials left the fields as they were
+            assert np.array_equal(s.get(k), before[k]), k
         s.step(10)
         for k in FIELDS:
-            assert np.array_equal(s.get(k).astype(np.float64), ref[k]), k
+            got = s.get(k).astype(np.float64)
+            if (v in PAIRS) == (v0 in PAIRS):  # the same arithmetic: bit for bit
+                assert np.array_equal(got, ref[k]), k
+            else:  # the other collide family: FP32 rounding apart
+                assert np.max(np.abs(got - ref[k])) < PAIR_TOL[storage][k], k
 
 
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
@@ -545,7 +554,7 @@ def test_errors_come_back_as_status_codes():
         assert e.value.code == mcb.ERR_INVALID
 
 
-def test_batch_autotune_restores_the_fields_and_matches_single_cases():
+def test_batch_autotune_restores_the_fields_and_matches_single_cases(tmp_path):
     """mcb_batch_autotune picks a tile variant and z chunk per size class. Afterwards the
     batch continues from the fields it had, and each case matches, bit for bit, a single
     handle run with that case's schedule."""
@@ -561,6 +570,7 @@ def test_batch_autotune_restores_the_fields_and_matches_single_cases():
             b.set_fields(i, phi, *u)
         b.step(3)
         before = [{k: b.get(i, k) for k in FIELDS} for i in range(len(cases))]
+        first = [b.schedule(i) for i in range(len(cases))]
         base, tuned = b.autotune(nsteps=4)
         assert tuned >= base > 0
         # the fields are those before the trials
@@ -572,8 +582,18 @@ def test_batch_autotune_restores_the_fields_and_matches_single_cases():
         assert sched[0] == sched[2] and sched[1] == sched[4], sched
         b.step(20)
         got = [{k: b.get(i, k) for k in FIELDS} for i in range(len(cases))]
+    # A single handle replays the case: 3 updates with the batch's first schedule, then (from
+    # a checkpoint) 20 with the tuned one.
     for i, (c, phi, u) in enumerate(cases):
+        ck = str(tmp_path / f"case{i}.ckpt")
+        c.variant, c.zchunk = first[i]
+        with mcb.Solver(c) as s:
+            s.set_fields(phi, *u)
+            s.step(3)
+            s.checkpoint_save(ck)
         c.variant, c.zchunk = sched[i]
-        single = gpu_run(c, phi, u, steps=23)
-        for k in FIELDS:
-            assert np.array_equal(got[i][k].astype(np.float64), single[k]), (i, sched[i], k)
+        with mcb.Solver(c) as s:
+            s.checkpoint_load(ck)
+            s.step(20)
+            for k in FIELDS:
+                assert np.array_equal(got[i][k], s.get(k)), (i, first[i], sched[i], k)
