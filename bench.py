@@ -601,6 +601,8 @@ def main():
                     help="tile variant of the device leg (-1 default; 4 the TMA-staged collide)")
     ap.add_argument("--zchunk", type=int, default=0,
                     help="work split of the device leg (0 default, >0 fixed chunks, -w waves)")
+    ap.add_argument("--tau-g", type=float, default=None,
+                    help="g relaxation time of the device leg (1: equilibrium g, the workload's)")
     ap.add_argument("--only-device", action="store_true",
                     help="time the device loop only (no fp16, e2e, reference or CPU legs)")
     args = ap.parse_args()
@@ -628,7 +630,7 @@ def main():
 
     with Clocks(local) as clk:
         cfg, total_ms, phi_ms, col_ms, diag = device_run(args.storage, local, args.steps,
-                                                         args.warmup, dist)
+                                                         args.warmup, dist, args.tau_g)
     t_max = reduce_max(dist, total_ms, dev)
     cells = cfg.nx * cfg.ny * cfg.nz
     value = ws * cells * args.steps / (t_max * 1e-3) / 1e6
@@ -657,7 +659,7 @@ def main():
                    "l2": f"inputs larger than L2 (f in and out: "
                          f"{2 * 19 * (4 if st == 'f32' else 2) * cells / 1e6:.0f} MB per update)",
                    "parallelism": f"replicas x{ws}", "seed": SEED},
-        "roofline": {"bound": "hbm", "kernel": KERNEL_OF[(st, None)], "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": KERNEL_OF[(st, args.tau_g)], "achieved": achieved,
                      "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": f"{peak_kind} HBM copy bandwidth",
