@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <array>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -589,12 +590,9 @@ struct Solver {
     MCB_TRY(set_device());
     mcb::CaseDesc& d = cases[ci];
     const size_t n = static_cast<size_t>(d.ncell);
-    double sum = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-      if (!std::isfinite(phi[i])) return fail(MCB_ERR_INVALID, "phi[%zu] is not finite", i);
-      sum += phi[i];
-    }
-    d.phi_mean = static_cast<float>(sum / static_cast<double>(n));
+    // The fields go to the staging buffer first; the device scans phi (its mean is the
+    // buoyancy reference, and a non-finite value rejects the call before any state
+    // changes). The one synchronisation also releases the caller's buffers.
     MCB_CU(cudaMemcpyAsync(stage, phi, n * sizeof(float), cudaMemcpyHostToDevice, stream));
     if (has_u) {
       MCB_CU(cudaMemcpyAsync(stage + n, ux, n * sizeof(float), cudaMemcpyHostToDevice, stream));
@@ -603,6 +601,16 @@ struct Solver {
       MCB_CU(cudaMemcpyAsync(stage + 3 * n, uz, n * sizeof(float), cudaMemcpyHostToDevice,
                              stream));
     }
+    MCB_CU(mcb::launch_field_scan(stage, static_cast<long long>(n), partials, result, stream));
+    struct {
+      double sum;
+      long long bad;
+    } scan{};
+    MCB_CU(cudaMemcpyAsync(&scan, result, sizeof scan, cudaMemcpyDeviceToHost, stream));
+    MCB_CU(cudaStreamSynchronize(stream));
+    if (scan.bad != LLONG_MAX)
+      return fail(MCB_ERR_INVALID, "phi[%lld] is not finite", scan.bad);
+    d.phi_mean = static_cast<float>(scan.sum / static_cast<double>(n));
     MCB_TRY(upload_tables());
     // A single case restarts from update 0 in buffer set 0.
     if (cases.size() == 1 || !stepped) {
@@ -632,8 +640,8 @@ struct Solver {
     a.cells_total = cells_total;
     a.gmode = gmode;
     a.qf = qf;
+    // Stream-ordered: the next call on the handle follows the init.
     MCB_CU(mcb::launch_init(storage, a, d.nx, d.ny, d.nz, stream));
-    MCB_CU(cudaStreamSynchronize(stream));
     fields_set[ci] = 1;
     return MCB_OK;
   }

@@ -1,5 +1,6 @@
 // Diagnostics reduction and the storage dispatch of the update kernels.
 #include <cfloat>
+#include <climits>
 #include <cstdint>
 #include <cstdio>
 
@@ -136,6 +137,59 @@ __global__ void k_diag_final(const DiagArgs a, int nparts) {
   *a.result = r;
 }
 
+// ------------------------------------------------- initial-field scan (set_fields) --
+
+// Sum and first non-finite index of n floats, on a fixed grid with a fixed reduction order
+// (the same result on every run): block b writes partial b, one thread then merges the
+// partials in block order.
+__global__ void __launch_bounds__(kDiagThreads)
+    k_field_scan(const float* v, long long n, double* psum, long long* pbad) {
+  double sum = 0.0;
+  long long bad = LLONG_MAX;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    const float x = v[i];
+    if (isfinite(x)) sum += x;
+    else bad = min(bad, i);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    sum += __shfl_down_sync(0xffffffffu, sum, off);
+    bad = min(bad, __shfl_down_sync(0xffffffffu, bad, off));
+  }
+  __shared__ double wsum[kDiagThreads / 32];
+  __shared__ long long wbad[kDiagThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    wsum[warp] = sum;
+    wbad[warp] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = wsum[0];
+    long long b = wbad[0];
+    for (int w = 1; w < kDiagThreads / 32; ++w) {
+      s += wsum[w];
+      b = min(b, wbad[w]);
+    }
+    psum[blockIdx.x] = s;
+    pbad[blockIdx.x] = b;
+  }
+}
+
+__global__ void k_field_scan_final(const double* psum, const long long* pbad, int nparts,
+                                   double* out_sum, long long* out_bad) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  long long b = LLONG_MAX;
+  for (int i = 0; i < nparts; ++i) {
+    s += psum[i];
+    b = min(b, pbad[i]);
+  }
+  *out_sum = s;
+  *out_bad = b;
+}
+
 // ------------------------------------------ allocation-free diagnostics (new kernels) --
 
 // The reduction of k_diag over caller-owned device fields, with sizes by value. P may be
@@ -253,6 +307,19 @@ cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
     case kStBF16: return launch_init_bf16(a, nx, ny, nz, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_field_scan(const float* v, long long n, void* partials, void* result,
+                              cudaStream_t s) {
+  double* psum = static_cast<double*>(partials);
+  long long* pbad = reinterpret_cast<long long*>(psum + kDiagBlocks);
+  double* out_sum = static_cast<double*>(result);
+  long long* out_bad = reinterpret_cast<long long*>(out_sum + 1);
+  k_field_scan<<<kDiagBlocks, kDiagThreads, 0, s>>>(v, n, psum, pbad);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_field_scan_final<<<1, 32, 0, s>>>(psum, pbad, kDiagBlocks, out_sum, out_bad);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s) {

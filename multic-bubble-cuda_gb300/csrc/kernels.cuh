@@ -1469,11 +1469,10 @@ __global__ void k_init(const InitArgs a) {
     const float fst = (S::kFDev && !ratio) ? feq - W : feq;
     const FT v = S::template f_put<L>(fst);
     f0[L * fn + fidx] = v;
-    f1[L * fn + fidx] = v;
-    if (fghost) {
-      f_ghosts<L>(f0, fn, x, y, z, nx, ny, cd->fgx, cd->fpx, cd->fpy, v);
-      f_ghosts<L>(f1, fn, x, y, z, nx, ny, cd->fgx, cd->fpx, cd->fpy, v);
-    }
+    // The first update writes every cell of the other buffer, except the reference-mode
+    // shell, whose f stays W_l in both buffers.
+    if (ref) f1[L * fn + fidx] = v;
+    if (fghost) f_ghosts<L>(f0, fn, x, y, z, nx, ny, cd->fgx, cd->fpx, cd->fpy, v);
     if (eq) {
       // no g populations are stored
     } else if constexpr (L == 0) {

@@ -124,7 +124,8 @@ __device__ __forceinline__ unsigned slot5(int v) { return static_cast<unsigned>(
 
 // kRef: some case of the launch is in reference mode (frozen shell); the shell handling is
 // compiled only into that instance, which also runs the other modes.
-template <class S, int BY, bool kRef>
+// kL2: prefetch into L2 the f rows of plane z + 2 while plane z collides.
+template <class S, int BY, bool kRef, bool kL2 = false>
 __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Tile& t) {
   using FT = typename S::FT;
   using IO = pk::PairIO<S>;
@@ -412,6 +413,28 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     __syncthreads();
     if (z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
     if (z + 2 <= t.ze) normals(z + 2);
+    if constexpr (kL2) {
+      // Plane z + 2 (the source plane of the next update's cz = -1 populations): rows
+      // yt - 1 .. yt + BY of the tile's two 32-cell blocks, each a contiguous run of
+      // 19 x 32 values, in 128-byte lines spread over the block's threads.
+      if (z + 2 < t.ze + 1) {
+        const int zq = t.bc == kBcPeriodic ? wrap1(z + 2, nz) : min(z + 2, nz - 1);
+        constexpr int kRunBytes = QF * 32 * static_cast<int>(sizeof(FT));
+        constexpr int kLines = (kRunBytes + 127) / 128;
+        constexpr int kJobs = (BY + 2) * 2 * kLines;
+        const char* pl = reinterpret_cast<const char*>(fin + static_cast<long long>(zq) * PS);
+        const int xb0 = t.xt >> 5;
+        for (int j = tid; j < kJobs; j += NT) {
+          const int line = j % kLines, rb = j / kLines;
+          const int row = rb >> 1, xb = xb0 + (rb & 1);
+          int yq = t.yt - 1 + row;
+          yq = yq < 0 ? yq + ny : (yq >= ny ? yq - ny : yq);
+          if (xb < t.fxb && yq >= 0 && yq < ny)
+            l2_prefetch(pl + (static_cast<long long>(yq) * RS + xb * (QF * 32)) * sizeof(FT) +
+                        line * 128);
+        }
+      }
+    }
     if (!active) continue;
 
     *reinterpret_cast<int2*>(pzero + idx) = make_int2(0, 0);  // next update accumulates here
@@ -633,24 +656,26 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
   for (int q = max(t.ze - 2, t.zb - 1); q <= t.ze; ++q) flush(q);
 }
 
-template <class S, int BY, bool kRef, int kMinBlocks>
+template <class S, int BY, bool kRef, int kMinBlocks, bool kL2 = false>
 __global__ void __launch_bounds__(kPairTX * BY, kMinBlocks)
     k_collide_pair(const StepArgs a) {
   for_each_segment<2 * kPairTX, BY, true>(
-      a, [&](const Tile& t) { collide_pair_segment<S, BY, kRef>(a, t); }, a.balanced != 0);
+      a, [&](const Tile& t) { collide_pair_segment<S, BY, kRef, kL2>(a, t); },
+      a.balanced != 0);
 }
 
 // The pair kernel of a tile variant, with or without the reference-mode shell handling.
 // Variant 5: three blocks of four warps per SM (168 registers: no spills, and more
 // independent work per warp; two blocks per SM measured 12 % slower at FP16 storage and 26 %
-// at FP32). Variant 6: four blocks per SM (128 registers).
+// at FP32, four blocks at 128 registers 6 % and 18 %). Variant 6: the same with an L2
+// prefetch of the f rows of the plane after next.
 template <class S>
 const void* pair_kernel(int variant, bool with_ref) {
   if (variant == kPairVariant)
     return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3>)
                     : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3>);
-  return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 4>)
-                  : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 4>);
+  return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3, true>)
+                  : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3, true>);
 }
 
 }  // namespace

@@ -162,6 +162,10 @@ cudaError_t occupancy(int storage, int variant, int gmode, int qf, int ratio, in
 cudaError_t launch_init(int storage, const InitArgs& a, int nx, int ny, int nz,
                         cudaStream_t s);
 cudaError_t launch_diag(const DiagArgs& a, cudaStream_t s);
+// Sum (FP64, fixed order) and first non-finite index (LLONG_MAX if none) of n device floats:
+// partials needs 2 * kDiagBlocks * 8 bytes, result receives {double sum, long long index}.
+cudaError_t launch_field_scan(const float* v, long long n, void* partials, void* result,
+                              cudaStream_t s);
 
 // Records msg as the calling thread's mcb_last_error() text; returns code.
 int report_error(int code, const char* msg);
