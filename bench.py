@@ -8,9 +8,11 @@ Workload: the rising perturbed bubble:
 A step is one lattice update of the whole lattice. Inputs exceed L2: the f populations one
 update reads and writes hold 638 MB.
 
-  value     MLUPS with the state resident in HBM: cells * K / device time of K updates,
-            CUDA events on the solver's stream, max over ranks. An event after every
-            kernel gives the per-kernel times of the same timed region.
+  value     MLUPS with the state resident in HBM: cells * K / device time of K updates as
+            the library runs them (CUDA-graph replay), CUDA events on the solver's stream,
+            max over ranks. Before the timed region: W warm-up updates and 34 untimed
+            updates that capture the graphs. A second pass of K updates with an event after
+            every kernel gives the per-kernel times of the roofline.
   e2e       the same metric through the C ABI with host buffers, timed on the host:
             upload of the initial fields from pinned memory, K updates, and a phi read-back
             every 100 updates (the reference's dump cadence, src/main.cu:184-189).
@@ -224,17 +226,26 @@ def collide_name(variant: int) -> str:
     return "k_collide_pair" if variant in PAIR_VARIANTS else "k_collide"
 
 
+GRAPH_PREP = 2 * 16 + 2  # untimed updates that capture both graph parities of 16 updates
+
+
 def device_run(storage, device, steps, warmup, dist, tau_g=None):
-    """Device-resident timing: K updates, an event after every kernel."""
+    """Device-resident timing. The timed region is K updates as the library runs them
+    (graph replay, CUDA events on the solver's stream); a second pass of K updates with an
+    event after every kernel gives the per-kernel times of the roofline."""
     s, cfg, fields = make_solver(storage, device, tau_g)
     KERNEL_OF[(storage, tau_g)] = collide_name(s.schedule[0])
     s.set_fields(*fields)
     s.step(warmup)
+    s.step(GRAPH_PREP)
     s.synchronize()
     barrier(dist)
-    total, t_phi, t_col = s.step_profiled(steps)
+    s.step(steps)
     s.synchronize()
+    total = s.last_step_ms()
     barrier(dist)
+    _, t_phi, t_col = s.step_profiled(steps)
+    s.synchronize()
     d = s.diagnostics(allow_nonfinite=True)
     s.close()
     return cfg, total, t_phi, t_col, d
@@ -658,7 +669,8 @@ def main():
                    "cells": cells,
                    "l2": f"inputs larger than L2 (f in and out: "
                          f"{2 * 19 * (4 if st == 'f32' else 2) * cells / 1e6:.0f} MB per update)",
-                   "parallelism": f"replicas x{ws}", "seed": SEED},
+                   "parallelism": f"replicas x{ws}", "seed": SEED,
+                   "graph_prep_updates": GRAPH_PREP},
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF[(st, args.tau_g)], "achieved": achieved,
                      "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
