@@ -416,23 +416,39 @@ struct Solver {
       max_blocked = std::max(max_blocked, ((d.nx + 31) / 32) * 32LL * d.ny * d.nz);
     const char* force_wide = std::getenv("MCB_WIDE_OFFSETS");
     wide = max_blocked * qf >= (1LL << 31) || (force_wide && force_wide[0] == '1');
-    // The two-cells-per-thread kernel: equilibrium g, D3Q19 f at density ratio 1, an even nx
-    // in every case. It addresses f per plane with 64-bit plane offsets, so it also runs the
-    // cases that need 64-bit f offsets, on the blocked layout.
-    pair_ok = gmode == mcb::kGEquil && qf == 19 && !ratio && !padded;
-    for (auto& d : cases)
+    // The two-cells-per-thread kernel: D3Q19 f at density ratio 1, an even nx in every case.
+    // It addresses f per plane with 64-bit plane offsets, so with equilibrium g it also runs
+    // the cases that need 64-bit f offsets, on the blocked layout. Stored g: periodic and
+    // wall modes, 32-bit g offsets (18 * cells < 2^31).
+    pair_ok = qf == 19 && !ratio && !padded;
+    for (auto& d : cases) {
       pair_ok = pair_ok && d.nx % 2 == 0 &&
                 (d.nx + 31LL) / 32 * 32 * d.ny * qf * static_cast<long long>(pop_bytes(storage)) <
                     (1LL << 32);  // a plane of f under 2^32 bytes
+      if (gmode != mcb::kGEquil)
+        pair_ok = pair_ok && d.bc != mcb::kBcRef && 18LL * d.ncell < (1LL << 31);
+    }
     if (mcb::is_pair_variant(variant) && !pair_ok) variant = 0;
-    // Default tile: the pair kernel where it applies (measured on GB300, 128x128x256 walls
-    // and gravity: 133 us against 137 at FP32, 120 against 138 at FP16 storage), else 32x8.
-    if (cs[0].variant < 0 && pair_ok) variant = mcb::kPairVariant;
+    // Default tile: the pair kernel where it applies, else 32x8. Measured on GB300, collide
+    // kernel of the 128x128x256 walls-and-gravity workload (FP32 / FP16 / BF16 storage):
+    //   - equilibrium g: 133 us against 137 at FP32, 120 against 138 at FP16;
+    //   - g stored at full relaxation: 163 / 147 / 156 us against 174 / 171 / 198;
+    //   - relaxed g (tau_g 0.8): 16-bit storage with the L2 prefetch variant, 275 / 303 us
+    //     against 298 / 313; at FP32 the one-cell tile stays (233 us against 286).
+    // Stored g takes the pair kernel from 2^21 cells: its blocks hold half the threads of
+    // the one-cell tile's, and the 64^3 static bubble (relaxed g) runs 47 / 52 us there
+    // against 39 / 41 one cell per thread at 16-bit storage.
+    if (cs[0].variant < 0 && pair_ok) {
+      if (gmode == mcb::kGEquil) variant = mcb::kPairVariant;
+      else if (cells_total >= (1LL << 21) && gmode == mcb::kGPop) variant = mcb::kPairVariant;
+      else if (cells_total >= (1LL << 21) && storage != MCB_STORE_F32)
+        variant = mcb::kPairVariant + 1;
+    }
     // f layout: blocked with equilibrium g and 32-bit offsets (x rounded up to whole 32-cell
     // blocks), or with the pair kernel at any size; plain otherwise (the 64-bit one-cell
     // kernels and the stored-g ones measured slower blocked: they spill the extra per-thread
-    // offsets). The padded TMA layout is set below.
-    const bool blocked = gmode == mcb::kGEquil && (!wide || mcb::is_pair_variant(variant));
+    // offsets, so they run the plain layout only). The padded TMA layout is set below.
+    const bool blocked = mcb::is_pair_variant(variant) || (gmode == mcb::kGEquil && !wide);
     wide_blocked = wide && blocked;
     f_cells_total = max_f_cells = 0;
     for (auto& d : cases) {
@@ -500,12 +516,14 @@ struct Solver {
   // Whether tile variant v can run these cases on the f layout fixed at creation: the TMA
   // variant alone on the padded layout; D3Q27 f and the density-ratio model on the 32x8
   // tile; the pair kernel where it applies, and alone on a blocked layout with 64-bit
-  // offsets.
+  // offsets. Stored g: the pair kernel on the blocked layout, the one-cell tiles on the
+  // plain one.
   bool variant_fits(int v) const {
     if ((v == mcb::kTmaVariant) != padded) return false;
     if ((qf == 27 || ratio) && v != 0) return false;
     if (mcb::is_pair_variant(v) && !pair_ok) return false;
     if (wide_blocked && !mcb::is_pair_variant(v)) return false;
+    if (gmode != mcb::kGEquil && mcb::is_pair_variant(v) != (cases[0].fxb > 0)) return false;
     return true;
   }
 

@@ -1506,10 +1506,12 @@ template <class S>
 const void* phi_kernel(int variant, bool eq, dim3* block) {
   switch (variant) {
     case 0:
-    case kPairVariant:
-    case kPairVariant + 1:
     case kTmaVariant: *block = dim3(32, 8); return phi_kernel_of<S, 32, 8>(eq);
     case 1: *block = dim3(16, 16); return phi_kernel_of<S, 16, 16>(eq);
+    // the pair variants' tiles are 64 x 4 cells (stored g runs this kernel on the first
+    // update of a push run)
+    case kPairVariant:
+    case kPairVariant + 1:
     case 2: *block = dim3(64, 4); return phi_kernel_of<S, 64, 4>(eq);
     case 3: *block = dim3(16, 8); return phi_kernel_of<S, 16, 8>(eq);
     default: return nullptr;
@@ -1525,14 +1527,10 @@ const void* collide_kernel(int variant, dim3* block) {
     case 3: *block = dim3(16, 8); return reinterpret_cast<const void*>(k_collide<S, GM, 16, 8>);
     case kPairVariant:
     case kPairVariant + 1:
-      // two cells per thread: equilibrium g only (the instance with the reference-mode
-      // shell, which runs every mode; launches pick by StepArgs::has_ref)
-      if constexpr (GM == kGEquil) {
-        *block = dim3(kPairTX, kPairBY);
-        return pair_kernel<S>(variant, false);
-      } else {
-        return nullptr;
-      }
+      // two cells per thread (the instance without the reference-mode shell; launches pick
+      // by StepArgs::has_ref)
+      *block = dim3(kPairTX, kPairBY);
+      return pair_kernel<S>(variant, false, GM);
     default: return nullptr;
   }
 }
@@ -1576,10 +1574,10 @@ const void* collide_kernel_gm(int variant, int gmode, dim3* block) {
 }
 
 inline cudaError_t launch_on(const void* fn, int grid, dim3 block, const StepArgs& a,
-                             cudaStream_t s) {
+                             cudaStream_t s, int dyn_smem = 0) {
   if (!fn || grid <= 0) return cudaErrorInvalidValue;
   void* args[] = {const_cast<StepArgs*>(&a)};
-  return cudaLaunchKernel(fn, dim3(grid), block, args, 0, s);
+  return cudaLaunchKernel(fn, dim3(grid), block, args, static_cast<size_t>(dyn_smem), s);
 }
 
 template <class S>
@@ -1628,8 +1626,18 @@ cudaError_t occupancy_of(int variant, int gmode, int qf, int ratio, int wide, in
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       phi_blocks, fp, static_cast<int>(bp.x * bp.y), 0);
   if (e != cudaSuccess) return e;
+  int dyn = 0;
+  if (is_pair_variant(variant)) {
+    // Every launch of a solver follows this call on its device: the opt-in above 48 KB of
+    // shared memory per block is set here.
+    dyn = pair_dyn_smem<S>(gmode);
+    if (dyn > 0) {
+      e = cudaFuncSetAttribute(fc, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (e != cudaSuccess) return e;
+    }
+  }
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(collide_blocks, fc,
-                                                       static_cast<int>(bc.x * bc.y), 0);
+                                                       static_cast<int>(bc.x * bc.y), dyn);
 }
 
 template <class S>
@@ -1654,9 +1662,8 @@ cudaError_t init_storage(const InitArgs& a, int nx, int ny, int nz, cudaStream_t
     if (variant == kTmaVariant)                                                            \
       return gmode == kGEquil ? launch_collide_tma<S>(a, tmap, s) : cudaErrorInvalidValue; \
     if (is_pair_variant(variant))                                                          \
-      return gmode == kGEquil ? launch_on(pair_kernel<S>(variant, a.has_ref != 0),          \
-                                          a.grid_collide, dim3(kPairTX, kPairBY), a, s)     \
-                              : cudaErrorInvalidValue;                                     \
+      return launch_on(pair_kernel<S>(variant, a.has_ref != 0, gmode), a.grid_collide,     \
+                       dim3(kPairTX, kPairBY), a, s, pair_dyn_smem<S>(gmode));             \
     if (a.qf == kQ27 || a.ratio || a.wide)                                                 \
       return launch_on(collide27_kernel<S>(gmode, a.qf, a.ratio != 0, a.wide != 0),        \
                        a.grid_collide, dim3(32, 8), a, s);                                 \

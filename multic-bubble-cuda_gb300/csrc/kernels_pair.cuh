@@ -40,6 +40,20 @@ __device__ __forceinline__ float2 addsg(float2 b, float2 a) {
   else return sub(b, a);
 }
 
+// Asynchronous B-byte copy (B = 4 or 8) from global to shared memory: the value goes
+// through no register, and cp_async_wait_all waits for this thread's copies.
+template <int B>
+__device__ __forceinline__ void cp_async(void* sdst, const void* gsrc) {
+  static_assert(B == 4 || B == 8, "cp.async.ca copies 4, 8 or 16 bytes");
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  const size_t g = __cvta_generic_to_global(gsrc);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(g), "n"(B)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Pair loads and stores of the storage formats. Deviation storage (16-bit) returns the
 // stored f - W; the moments add the weights' moments.
 template <class S>
@@ -112,6 +126,56 @@ struct PairIO<mcb::StB16> {
   }
 };
 
+// Stored g of a pair of cells: raw loads, and the store of both cells' encoded values.
+template <class S>
+struct GPairIO;
+template <>
+struct GPairIO<mcb::StF32> {
+  using GT = int;  // Q2.30
+  using R2 = int2;
+  using R1 = int;
+  static __device__ __forceinline__ R2 raw2(const int* p) {
+    return __ldg(reinterpret_cast<const int2*>(p));
+  }
+  static __device__ __forceinline__ R1 raw1(const int* p) { return __ldg(p); }
+  static __device__ __forceinline__ R1 lo(R2 v) { return v.x; }
+  static __device__ __forceinline__ R1 hi(R2 v) { return v.y; }
+  static __device__ __forceinline__ void st2(int* p, int a, int b) {
+    *reinterpret_cast<int2*>(p) = make_int2(a, b);
+  }
+};
+template <>
+struct GPairIO<mcb::StH16> {
+  using GT = __half;
+  using R2 = __half2;
+  using R1 = __half;
+  static __device__ __forceinline__ R2 raw2(const __half* p) {
+    return __ldg(reinterpret_cast<const __half2*>(p));
+  }
+  static __device__ __forceinline__ R1 raw1(const __half* p) { return __ldg(p); }
+  static __device__ __forceinline__ R1 lo(R2 v) { return __low2half(v); }
+  static __device__ __forceinline__ R1 hi(R2 v) { return __high2half(v); }
+  static __device__ __forceinline__ void st2(__half* p, __half a, __half b) {
+    *reinterpret_cast<__half2*>(p) = __halves2half2(a, b);
+  }
+};
+template <>
+struct GPairIO<mcb::StB16> {
+  using GT = __nv_bfloat16;
+  using R2 = __nv_bfloat162;
+  using R1 = __nv_bfloat16;
+  static __device__ __forceinline__ R2 raw2(const __nv_bfloat16* p) {
+    return __ldg(reinterpret_cast<const __nv_bfloat162*>(p));
+  }
+  static __device__ __forceinline__ R1 raw1(const __nv_bfloat16* p) { return __ldg(p); }
+  static __device__ __forceinline__ R1 lo(R2 v) { return __low2bfloat16(v); }
+  static __device__ __forceinline__ R1 hi(R2 v) { return __high2bfloat16(v); }
+  static __device__ __forceinline__ void st2(__nv_bfloat16* p, __nv_bfloat16 a,
+                                             __nv_bfloat16 b) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __halves2bfloat162(a, b);
+  }
+};
+
 }  // namespace pk
 
 namespace mcb {
@@ -122,11 +186,31 @@ constexpr int kPairTX = 32;  // threads in x; a tile is 2 * kPairTX = 64 cells w
 // Ring slot of a non-negative plane index in the 5-plane phi ring (unsigned: no sign fix-up).
 __device__ __forceinline__ unsigned slot5(int v) { return static_cast<unsigned>(v) % 5u; }
 
+// Dynamic shared memory of the relaxed-g pair kernel: two planes of staged g (18
+// populations x kPairBY rows x 34 words of two cells) and, for the 16-bit deviation form, a
+// ring of four planes of staged previous phi (kPairBY + 2 rows x 34 words).
+template <class S>
+__host__ __device__ constexpr int pair_gbuf_bytes() {
+  return 2 * (kQ - 1) * kPairBY * 2 * (kPairTX + 2) * static_cast<int>(sizeof(typename S::GT));
+}
+template <class S>
+__host__ __device__ constexpr int pair_bgk_smem() {
+  return pair_gbuf_bytes<S>() + (S::kDev ? 4 * (kPairBY + 2) * 2 * (kPairTX + 2) * 4 : 0);
+}
+
 // kRef: some case of the launch is in reference mode (frozen shell); the shell handling is
 // compiled only into that instance, which also runs the other modes.
 // kL2: prefetch into L2 the f rows of plane z + 2 while plane z collides.
-template <class S, int BY, bool kRef, bool kL2 = false>
+// GM: how g crosses the update (kGEquil: pushed equilibrium populations, nothing stored;
+// kGPop: stored at full relaxation; kGBgk: stored, pulled and relaxed with tau_g != 1). The
+// stored forms run periodic and wall modes only (no reference shell) and need 18 * cells
+// below 2^31 (checked on the host).
+template <class S, int BY, bool kRef, bool kL2, int GM>
 __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Tile& t) {
+  constexpr bool EQ = GM == kGEquil;
+  constexpr bool BGK = GM == kGBgk;
+  using GIO = pk::GPairIO<S>;
+  using GT = typename GIO::GT;
   using FT = typename S::FT;
   using IO = pk::PairIO<S>;
   using pk::add;
@@ -156,7 +240,7 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
   const bool active = x0 < nx && y < ny;  // nx is even: x0 + 1 < nx with x0
 
   const CaseDesc* cd = a.cases + t.ci;
-  const float omega = __ldg(&cd->omega);
+  const float omega = __ldg(&cd->omega), omega_g = __ldg(&cd->omega_g);
   const float sigma = __ldg(&cd->sigma), sharp_c = __ldg(&cd->sharp_c);
   const float gravity = __ldg(&cd->gravity), phi_mean = __ldg(&cd->phi_mean);
 
@@ -337,6 +421,70 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     if constexpr (cx(L) == 0) return IO::cvt2(r2[L]);
     else return make_float2(IO::cvt1(r1a[L]), IO::cvt1(r1b[L]));
   };
+  // Stored g.
+  const GT* __restrict__ gin = static_cast<const GT*>(a.g_in) + t.g_off;
+  GT* __restrict__ gout = static_cast<GT*>(a.g_out) + t.g_off;
+  const int* __restrict__ pprev = a.p_prev + t.cell_off;
+  const int ng = static_cast<int>(t.ncell);
+  // Relaxed g pulls the 18 stored populations of its sources; the 16-bit form decodes each
+  // against its source's previous phi. Both are staged in shared memory with asynchronous
+  // copies one plane ahead, so that no register holds them across the plane's barrier:
+  //   - g of plane z: per population and tile row, the source row's words (2 cells each)
+  //     from x = xt - 2 to xt + 64 (words 0 .. TX + 1), in two buffers (z & 1);
+  //   - previous phi: rows yt - 1 .. yt + BY of a plane, the same x range, in a ring of
+  //     four planes (q & 3): planes z - 1 .. z + 1 are read while z + 2 arrives.
+  // Element 2 tx + 2 - cx of a staged row is the source x0 - cx of the pair's first cell.
+  constexpr int GW = TX + 2, GR = 2 * GW;  // words and elements of a staged row
+  constexpr int PR = BY + 2;               // staged previous-phi rows
+  extern __shared__ __align__(16) unsigned char pair_dyn[];
+  GT* const gbuf = reinterpret_cast<GT*>(pair_dyn);
+  int* const pring = reinterpret_cast<int*>(pair_dyn + pair_gbuf_bytes<S>());
+  // A staged coordinate one step or so past the lattice edge, wrapped (the reads that use
+  // it); coordinates further out are never read and take 0.
+  auto wrap_st = [](int v, int n) { return v < 0 ? v + n : (v < n ? v : (v - n < n ? v - n : 0)); };
+  constexpr int KPJ = (PR * GW + NT - 1) / NT;  // previous-phi words per thread and plane
+  auto gplane = [&](int q) {  // the stored plane of plane index q (walls: clamped, unread)
+    if (t.bc == kBcPeriodic) q = wrap1(q, nz);
+    return clampi(q, 0, nz - 1) * nxy;
+  };
+  constexpr int kGW = 2 * static_cast<int>(sizeof(GT));  // bytes of a g word
+  // Copies the g words of collision plane zq into buffer zq & 1.
+  // Each thread copies, for its row y, the word at x0 of the rows y - 1, y, y + 1 (the
+  // first thread past the lattice edge in x: the wrapped word at x = 0); thread 0 adds the
+  // left halo word, thread TX - 1 the right one. Rows past the edge are never read.
+  auto stage_g = [&](int zq) {
+    const int zs[3] = {gplane(zq - 1), gplane(zq), gplane(zq + 1)};  // cz = 1, 0, -1
+    const int yr = y < ny ? y : 0;
+    const int rows[3] = {(yr == 0 ? ny - 1 : yr - 1) * nx, yr * nx,  // cy = 1, 0, -1
+                         (yr == ny - 1 ? 0 : yr + 1) * nx};
+    const int xo = x0 < nx ? x0 : 0;
+    const int xh = wrap_st(tx == 0 ? t.xt - 2 : t.xt + 2 * TX, nx);
+    GT* b = gbuf + (zq & 1) * ((kQ - 1) * BY * GR) + ty * GR;
+    static_for<1, kQ>([&](auto LC) {
+      constexpr int L = decltype(LC)::value;
+      const GT* src = gin + (L - 1) * ng + zs[1 - cz(L)] + rows[1 - cy(L)];
+      GT* dst = b + (L - 1) * (BY * GR);
+      pk::cp_async<kGW>(dst + 2 + 2 * tx, src + xo);
+      if constexpr (cx(L) == 1) {
+        if (tx == 0) pk::cp_async<kGW>(dst, src + xh);
+      } else if constexpr (cx(L) == -1) {
+        if (tx == TX - 1) pk::cp_async<kGW>(dst + 2 * (TX + 1), src + xh);
+      }
+    });
+  };
+  // Copies the previous phi of plane q into ring slot q & 3.
+  auto stage_p = [&](int q) {
+    const int* src = pprev + gplane(q);
+    int* dst = pring + (q & 3) * (PR * GR);
+#pragma unroll
+    for (int k = 0; k < KPJ; ++k) {
+      const int j = tid + k * NT;
+      if ((k + 1) * NT <= PR * GW || j < PR * GW)
+        pk::cp_async<8>(dst + 2 * j, src + wrap_st(t.yt - 1 + j / GW, ny) * nx +
+                                          wrap_st(t.xt - 2 + 2 * (j % GW), nx));
+    }
+  };
+
   // Gathers the 19 populations of both cells of plane z and their Q2.30 phi.
   auto gather = [&](int z, int2& pcv) {
     const bool blo = walls && z == 0, bhi = walls && z == nz - 1;
@@ -398,6 +546,11 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
   int2 pc = make_int2(0, 0);
   __syncthreads();
   for (int zpl = t.zb - 1; zpl <= t.zb + 1; ++zpl) normals(zpl);
+  if constexpr (BGK) {
+    stage_g(t.zb);
+    if constexpr (S::kDev)
+      for (int q = t.zb - 1; q <= t.zb + 1; ++q) stage_p(q);
+  }
   __syncthreads();
 
   for (int z = t.zb; z < t.ze; ++z) {
@@ -410,7 +563,16 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     // The gathered values stay as loaded until the moments use them, after the barrier and
     // the normals: no instruction waits on these loads before then.
     if (active) gather(z, pc);
+    if constexpr (BGK) pk::cp_async_wait_all();  // this plane's staged g and previous phi
     __syncthreads();
+    if constexpr (BGK) {
+      // The next plane's: its buffers were last read by plane z - 1, which every thread
+      // has finished.
+      if (z + 1 < t.ze) {
+        stage_g(z + 1);
+        if constexpr (S::kDev) stage_p(z + 2);
+      }
+    }
     if (z - 2 >= t.zb - 1) flush(z - 2);  // complete: sources z-3 .. z-1 are in
     if (z + 2 <= t.ze) normals(z + 2);
     if constexpr (kL2) {
@@ -514,6 +676,74 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     // Regularized collision with He forcing (collisionFluid, src/lbm.cu:233-288):
     //   f*_l = W_l [E_l (rho + 3/2 (c_l.F - u.F)) + 9/2 (1 - omega) Q_l:Pi]
     // per opposite pair, with E_l = 1 + 3 c.u + 9/2 (c.u)^2 - 3/2 u^2.
+    // g: A and 3 phi for the equilibrium W_l (phi + 3 phi c.u + A c.n)
+    const float2 A = mul(scale(phi, sharp_c), fma(dup(-1.0f), phi, dup(1.0f)));
+    const float2 phi3 = scale(phi, 3.0f);
+    // Ring offsets of the pair's own row in the three target planes of the push.
+    int* s0 = &sacc[(z + 8) & 3][h0];
+    int* sm = &sacc[(z + 7) & 3][h0];
+    int* sp = &sacc[(z + 9) & 3][h0];
+    // Stored g: each population is encoded, stored and pushed as the collision makes it
+    // (collisionPhase, src/lbm.cu:290-329; BGK with omega_g when tau_g != 1). The 16-bit
+    // form stores it relative to the split of this cell's phi.
+    const GSplit gsp0 = S::g_split(pc.x), gsp1 = S::g_split(pc.y);
+    int sumq0 = 0, sumq1 = 0;
+    auto emit = [&](auto LC, float2 g) {
+      constexpr int L = decltype(LC)::value;
+      int qa, qb;
+      const GT ha = S::template g_put<L>(g.x, gsp0, qa);
+      const GT hb = S::template g_put<L>(g.y, gsp1, qb);
+      GIO::st2(gout + (L - 1) * ng + idx, ha, hb);
+      sumq0 += qa;
+      sumq1 += qb;
+      constexpr int D = cy(L) * HX + cx(L);
+      const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
+      int* tgt = bounce ? s0 : (cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0)) + D;
+      atomicAdd(tgt, qa);
+      atomicAdd(tgt + 1, qb);
+    };
+    // The decoded incoming population L of both cells (relaxed g): staged, or across a z
+    // wall the cell's own opposite population.
+    auto gdec = [&](auto LC) -> float2 {
+      constexpr int L = decltype(LC)::value;
+      constexpr int O = opp(L);
+      const bool bounce = (cz(L) == 1) ? blo : ((cz(L) == -1) ? bhi : false);
+      int ia, ib;
+      if (bounce) {
+        const typename GIO::R2 v = GIO::raw2(gin + (O - 1) * ng + idx);
+        int2 ps = make_int2(0, 0);
+        if constexpr (S::kDev) ps = __ldg(reinterpret_cast<const int2*>(pprev + idx));
+        ia = S::template g_dec<O>(GIO::lo(v), ps.x);
+        ib = S::template g_dec<O>(GIO::hi(v), ps.y);
+      } else {
+        constexpr int e = 2 - cx(L);  // the first cell's source, less 2 tx
+        const GT* gr = gbuf + ((z & 1) * (kQ - 1) + (L - 1)) * (BY * GR) + ty * GR + 2 * tx + e;
+        GT va, vb;
+        if constexpr (cx(L) == 0) {
+          const typename GIO::R2 w = *reinterpret_cast<const typename GIO::R2*>(gr);
+          va = GIO::lo(w);
+          vb = GIO::hi(w);
+        } else {
+          va = gr[0];
+          vb = gr[1];
+        }
+        int pa = 0, pb = 0;
+        if constexpr (S::kDev) {
+          const int* pr = pring + ((z - cz(L)) & 3) * (PR * GR) + (ty + 1 - cy(L)) * GR + 2 * tx + e;
+          if constexpr (cx(L) == 0) {
+            const int2 w = *reinterpret_cast<const int2*>(pr);
+            pa = w.x;
+            pb = w.y;
+          } else {
+            pa = pr[0];
+            pb = pr[1];
+          }
+        }
+        ia = S::template g_dec<L>(va, pa);
+        ib = S::template g_dec<L>(vb, pb);
+      }
+      return scale(make_float2(__int2float_rn(ia), __int2float_rn(ib)), kInvQ30);
+    };
     const float2 om = dup((1.0f - omega) * 4.5f);
     constexpr float fshift = kDevF ? -1.0f : 0.0f;
     const float2 R = add(rho, nh);
@@ -549,86 +779,108 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
       put(L, scale(fma(add(e0, e1), add(R, rf), q), W));
       put(O, scale(fma(sub(e0, e1), sub(R, rf), q), W));
     });
-
-    // g (collisionPhase, src/lbm.cu:290-329), full relaxation: the populations are the
-    // equilibrium W_l (phi + c_l.J), J = 3 phi u + sharp_c phi (1 - phi) n, pushed as exact
-    // Q2.30 integers into the next phi (streamingCalc + phiCalc).
-    const float2 A = mul(scale(phi, sharp_c), fma(dup(-1.0f), phi, dup(1.0f)));
-    const float2 phi3 = scale(phi, 3.0f);
-    constexpr float kj = 1073741824.0f / 36.0f;
-    const float2 Jx = scale(fma(phi3, ux, mul(A, ncx)), kj);
-    const float2 Jy = scale(fma(phi3, uy, mul(A, ncy)), kj);
-    const float2 Jz = scale(fma(phi3, uz, mul(A, ncz)), kj);
-    // shell lanes push their phi with no flux
-    JQ j0{__float2int_rn(Jx.x), __float2int_rn(Jy.x), __float2int_rn(Jz.x)};
-    JQ j1{__float2int_rn(Jx.y), __float2int_rn(Jy.y), __float2int_rn(Jz.y)};
-    if (kRef) {
-      if (sh0) j0 = JQ{0, 0, 0};
-      if (sh1) j1 = JQ{0, 0, 0};
+    if constexpr (!EQ) {
+      // Stored g, after the f collision (fewer values live at once): W_l (phi +- dg),
+      // dg = 3 phi c.u + A c.n, relaxed against the pulled populations (tau_g != 1).
+      static_for<0, (kQ - 1) / 2>([&](auto KC) {
+        constexpr int L = 2 * decltype(KC)::value + 1;
+        constexpr int O = L + 1;
+        constexpr float WG = wf(L);
+        float2 cu = dup(0.f), cn = dup(0.f);
+        if constexpr (cx(L) != 0) { cu = pk::addsg<cx(L)>(cu, ux); cn = pk::addsg<cx(L)>(cn, ncx); }
+        if constexpr (cy(L) != 0) { cu = pk::addsg<cy(L)>(cu, uy); cn = pk::addsg<cy(L)>(cn, ncy); }
+        if constexpr (cz(L) != 0) { cu = pk::addsg<cz(L)>(cu, uz); cn = pk::addsg<cz(L)>(cn, ncz); }
+        const float2 dg = fma(phi3, cu, mul(A, cn));
+        float2 gL = scale(add(phi, dg), WG), gO = scale(sub(phi, dg), WG);
+        if constexpr (BGK) {
+          const float2 fL = gdec(std::integral_constant<int, L>{});
+          const float2 fO = gdec(std::integral_constant<int, O>{});
+          gL = fma(dup(omega_g), sub(gL, fL), fL);
+          gO = fma(dup(omega_g), sub(gO, fO), fO);
+        }
+        emit(std::integral_constant<int, L>{}, gL);
+        emit(std::integral_constant<int, O>{}, gO);
+      });
+      // the rest population: the exact remainder of each cell's phi
+      atomicAdd(s0, pc.x - sumq0);
+      atomicAdd(s0 + 1, pc.y - sumq1);
     }
-    {
-      const int wf0 = wsplit_face(pc.x), we0 = wsplit_edge_of_face(wf0);
-      const int wf1 = wsplit_face(pc.y), we1 = wsplit_edge_of_face(wf1);
-      auto q0 = [&](auto LC) -> int {
-        constexpr int L = decltype(LC)::value;
-        if constexpr (L == 0) return pc.x - 6 * wf0 - 12 * we0;
-        else return (L <= 6 ? wf0 : we0) + qj<L>(j0);
-      };
-      auto q1 = [&](auto LC) -> int {
-        constexpr int L = decltype(LC)::value;
-        if constexpr (L == 0) return pc.y - 6 * wf1 - 12 * we1;
-        else return (L <= 6 ? wf1 : we1) + qj<L>(j1);
-      };
-      // Ring offsets of the pair's own row in the three target planes.
-      int* s0 = &sacc[(z + 8) & 3][h0];
-      int* sm = &sacc[(z + 7) & 3][h0];
-      int* sp = &sacc[(z + 9) & 3][h0];
-      if (walls && (blo || bhi)) {
-        // A wall plane: what leaves through the wall returns to the cell itself.
-        static_for<0, kQ>([&](auto LC) {
+
+    if constexpr (EQ) {
+      // g (collisionPhase, src/lbm.cu:290-329), full relaxation: the populations are the
+      // equilibrium W_l (phi + c_l.J), J = 3 phi u + sharp_c phi (1 - phi) n, pushed as exact
+      // Q2.30 integers into the next phi (streamingCalc + phiCalc).
+      constexpr float kj = 1073741824.0f / 36.0f;
+      const float2 Jx = scale(fma(phi3, ux, mul(A, ncx)), kj);
+      const float2 Jy = scale(fma(phi3, uy, mul(A, ncy)), kj);
+      const float2 Jz = scale(fma(phi3, uz, mul(A, ncz)), kj);
+      // shell lanes push their phi with no flux
+      JQ j0{__float2int_rn(Jx.x), __float2int_rn(Jy.x), __float2int_rn(Jz.x)};
+      JQ j1{__float2int_rn(Jx.y), __float2int_rn(Jy.y), __float2int_rn(Jz.y)};
+      if (kRef) {
+        if (sh0) j0 = JQ{0, 0, 0};
+        if (sh1) j1 = JQ{0, 0, 0};
+      }
+      {
+        const int wf0 = wsplit_face(pc.x), we0 = wsplit_edge_of_face(wf0);
+        const int wf1 = wsplit_face(pc.y), we1 = wsplit_edge_of_face(wf1);
+        auto q0 = [&](auto LC) -> int {
           constexpr int L = decltype(LC)::value;
-          constexpr int D = cy(L) * HX + cx(L);
-          const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
-          int* tgt = cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0);
-          atomicAdd(bounce ? s0 : tgt + D, q0(LC));
-          atomicAdd(bounce ? s0 + 1 : tgt + D + 1, q1(LC));
-        });
-      } else {
-        // Targets of the pair in one (cy, cz) row: cell x0 reaches h0 - 1 .. h0 + 1, cell
-        // x0 + 1 reaches h0 .. h0 + 2. The two middle targets take one atomic each for
-        // both cells.
-        auto row = [&](int* b, auto LM, auto L0, auto LP) {
-          constexpr int Z = decltype(L0)::value;
-          // LM: cx = -1, L0: cx = 0, LP: cx = +1 (each of the same cy, cz)
-          atomicAdd(b - 1, q0(LM));
-          atomicAdd(b, q0(std::integral_constant<int, Z>{}) + q1(LM));
-          atomicAdd(b + 1, q0(LP) + q1(std::integral_constant<int, Z>{}));
-          atomicAdd(b + 2, q1(LP));
+          if constexpr (L == 0) return pc.x - 6 * wf0 - 12 * we0;
+          else return (L <= 6 ? wf0 : we0) + qj<L>(j0);
         };
-        // rest, +x, -x in the cell's own row and plane
-        row(s0, std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
-            std::integral_constant<int, 1>{});
-        // rows y+1 and y-1 in the plane: (-1,+1,0) 14, (0,+1,0) 3, (+1,+1,0) 7;
-        // (-1,-1,0) 8, (0,-1,0) 4, (+1,-1,0) 13
-        row(s0 + HX, std::integral_constant<int, 14>{}, std::integral_constant<int, 3>{},
-            std::integral_constant<int, 7>{});
-        row(s0 - HX, std::integral_constant<int, 8>{}, std::integral_constant<int, 4>{},
-            std::integral_constant<int, 13>{});
-        // planes z+1 and z-1: (-1,0,+1) 16, (0,0,+1) 5, (+1,0,+1) 9;
-        // (-1,0,-1) 10, (0,0,-1) 6, (+1,0,-1) 15
-        row(sp, std::integral_constant<int, 16>{}, std::integral_constant<int, 5>{},
-            std::integral_constant<int, 9>{});
-        row(sm, std::integral_constant<int, 10>{}, std::integral_constant<int, 6>{},
-            std::integral_constant<int, 15>{});
-        // the four (0, +-1, +-1) edges: one target per cell
-        static_for<0, 4>([&](auto KC) {
-          constexpr int K = decltype(KC)::value;
-          constexpr int L = K == 0 ? 11 : (K == 1 ? 12 : (K == 2 ? 17 : 18));
-          constexpr int D = cy(L) * HX;
-          int* b = (cz(L) > 0 ? sp : sm) + D;
-          atomicAdd(b, q0(std::integral_constant<int, L>{}));
-          atomicAdd(b + 1, q1(std::integral_constant<int, L>{}));
-        });
+        auto q1 = [&](auto LC) -> int {
+          constexpr int L = decltype(LC)::value;
+          if constexpr (L == 0) return pc.y - 6 * wf1 - 12 * we1;
+          else return (L <= 6 ? wf1 : we1) + qj<L>(j1);
+        };
+        if (walls && (blo || bhi)) {
+          // A wall plane: what leaves through the wall returns to the cell itself.
+          static_for<0, kQ>([&](auto LC) {
+            constexpr int L = decltype(LC)::value;
+            constexpr int D = cy(L) * HX + cx(L);
+            const bool bounce = cz(L) < 0 ? blo : (cz(L) > 0 ? bhi : false);
+            int* tgt = cz(L) < 0 ? sm : (cz(L) > 0 ? sp : s0);
+            atomicAdd(bounce ? s0 : tgt + D, q0(LC));
+            atomicAdd(bounce ? s0 + 1 : tgt + D + 1, q1(LC));
+          });
+        } else {
+          // Targets of the pair in one (cy, cz) row: cell x0 reaches h0 - 1 .. h0 + 1, cell
+          // x0 + 1 reaches h0 .. h0 + 2. The two middle targets take one atomic each for
+          // both cells.
+          auto row = [&](int* b, auto LM, auto L0, auto LP) {
+            constexpr int Z = decltype(L0)::value;
+            // LM: cx = -1, L0: cx = 0, LP: cx = +1 (each of the same cy, cz)
+            atomicAdd(b - 1, q0(LM));
+            atomicAdd(b, q0(std::integral_constant<int, Z>{}) + q1(LM));
+            atomicAdd(b + 1, q0(LP) + q1(std::integral_constant<int, Z>{}));
+            atomicAdd(b + 2, q1(LP));
+          };
+          // rest, +x, -x in the cell's own row and plane
+          row(s0, std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{},
+              std::integral_constant<int, 1>{});
+          // rows y+1 and y-1 in the plane: (-1,+1,0) 14, (0,+1,0) 3, (+1,+1,0) 7;
+          // (-1,-1,0) 8, (0,-1,0) 4, (+1,-1,0) 13
+          row(s0 + HX, std::integral_constant<int, 14>{}, std::integral_constant<int, 3>{},
+              std::integral_constant<int, 7>{});
+          row(s0 - HX, std::integral_constant<int, 8>{}, std::integral_constant<int, 4>{},
+              std::integral_constant<int, 13>{});
+          // planes z+1 and z-1: (-1,0,+1) 16, (0,0,+1) 5, (+1,0,+1) 9;
+          // (-1,0,-1) 10, (0,0,-1) 6, (+1,0,-1) 15
+          row(sp, std::integral_constant<int, 16>{}, std::integral_constant<int, 5>{},
+              std::integral_constant<int, 9>{});
+          row(sm, std::integral_constant<int, 10>{}, std::integral_constant<int, 6>{},
+              std::integral_constant<int, 15>{});
+          // the four (0, +-1, +-1) edges: one target per cell
+          static_for<0, 4>([&](auto KC) {
+            constexpr int K = decltype(KC)::value;
+            constexpr int L = K == 0 ? 11 : (K == 1 ? 12 : (K == 2 ? 17 : 18));
+            constexpr int D = cy(L) * HX;
+            int* b = (cz(L) > 0 ? sp : sm) + D;
+            atomicAdd(b, q0(std::integral_constant<int, L>{}));
+            atomicAdd(b + 1, q1(std::integral_constant<int, L>{}));
+          });
+        }
       }
     }
     if (kRef && (sh0 || sh1)) {
@@ -656,11 +908,11 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
   for (int q = max(t.ze - 2, t.zb - 1); q <= t.ze; ++q) flush(q);
 }
 
-template <class S, int BY, bool kRef, int kMinBlocks, bool kL2 = false>
+template <class S, int BY, bool kRef, int kMinBlocks, bool kL2, int GM>
 __global__ void __launch_bounds__(kPairTX * BY, kMinBlocks)
     k_collide_pair(const StepArgs a) {
   for_each_segment<2 * kPairTX, BY, true>(
-      a, [&](const Tile& t) { collide_pair_segment<S, BY, kRef, kL2>(a, t); },
+      a, [&](const Tile& t) { collide_pair_segment<S, BY, kRef, kL2, GM>(a, t); },
       a.balanced != 0);
 }
 
@@ -669,13 +921,38 @@ __global__ void __launch_bounds__(kPairTX * BY, kMinBlocks)
 // independent work per warp; two blocks per SM measured 12 % slower at FP16 storage and 26 %
 // at FP32, four blocks at 128 registers 6 % and 18 %). Variant 6: the same with an L2
 // prefetch of the f rows of the plane after next.
+template <class S, int GM>
+const void* pair_kernel_gm(int variant, bool with_ref) {
+  if constexpr (GM != kGEquil) {
+    // stored g: periodic and wall modes only (the host sees to it)
+    // relaxed FP32 g: its staged planes leave room for two blocks per SM
+    constexpr int MB = (GM == kGBgk && !S::kDev) ? 2 : 3;
+    return variant == kPairVariant
+               ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, MB, false, GM>)
+               : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, MB, true, GM>);
+  } else if (variant == kPairVariant) {
+    return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3, false, GM>)
+                    : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3, false, GM>);
+  } else {
+    return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3, true, GM>)
+                    : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3, true, GM>);
+  }
+}
+
+// Dynamic shared memory of a pair-kernel launch.
 template <class S>
-const void* pair_kernel(int variant, bool with_ref) {
-  if (variant == kPairVariant)
-    return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3>)
-                    : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3>);
-  return with_ref ? reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, true, 3, true>)
-                  : reinterpret_cast<const void*>(k_collide_pair<S, kPairBY, false, 3, true>);
+int pair_dyn_smem(int gmode) {
+  return gmode == kGBgk ? pair_bgk_smem<S>() : 0;
+}
+
+template <class S>
+const void* pair_kernel(int variant, bool with_ref, int gmode) {
+  switch (gmode) {
+    case kGEquil: return pair_kernel_gm<S, kGEquil>(variant, with_ref);
+    case kGBgk: return pair_kernel_gm<S, kGBgk>(variant, with_ref);
+    case kGPop: return pair_kernel_gm<S, kGPop>(variant, with_ref);
+    default: return nullptr;
+  }
 }
 
 }  // namespace

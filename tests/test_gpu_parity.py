@@ -185,13 +185,16 @@ def test_16bit_storage_stays_close_to_fp64(storage, tol):
 def test_tile_variants_graphs_and_chunks_agree_bitwise():
     cfg, phi, u = small_case(mcb.BC_WALLS_Z, n=(40, 36, 30), tau_g=0.8, gravity=1e-4,
                              noise=1e-3)
-    base = gpu_run(cfg, phi, u, steps=41, variant=0, use_graph=0, zchunk=0)
+    # the one-cell tiles against the 32x8 one, the pair variants against each other
+    base = {0: gpu_run(cfg, phi, u, steps=41, variant=0, use_graph=0, zchunk=0),
+            PAIR: gpu_run(cfg, phi, u, steps=41, variant=PAIR, use_graph=0, zchunk=0)}
     for v in range(mcb.lib().mcb_variant_count()):
         for g in (0, 1):
             for zc in (0, -3, 4, 7):
                 r = gpu_run(cfg, phi, u, steps=41, variant=v, use_graph=g, zchunk=zc)
+                want = base[PAIR if v in PAIRS else 0]
                 for k in FIELDS:
-                    assert np.array_equal(r[k], base[k]), (v, g, zc, k)
+                    assert np.array_equal(r[k], want[k]), (v, g, zc, k)
 
 
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
@@ -230,11 +233,25 @@ def test_tma_collide_is_skipped_where_it_does_not_apply():
     cfg.variant = 4
     with mcb.Solver(cfg) as s:
         assert s.schedule[0] == 0
-    # the default is the two-cells-per-thread tile where it applies, else the 32x8 tile
-    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30))
-    with mcb.Solver(cfg) as s:
-        assert s.schedule[0] == PAIR
-    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(48, 20, 30), tau_g=0.8)
+    # The default is the two-cells-per-thread tile where it applies, else the 32x8 tile.
+    # Stored g takes it from 2^21 cells (relaxed g: with the L2 prefetch at 16-bit storage,
+    # not at all at FP32).
+    big = (128, 128, 128)
+    for n, tau_g, g_mode, storage, want in (
+            ((48, 20, 30), 1.0, mcb.G_AUTO, mcb.STORE_F32, PAIR),
+            ((48, 20, 30), 1.0, mcb.G_POPULATIONS, mcb.STORE_F16, 0),
+            ((48, 20, 30), 0.8, mcb.G_AUTO, mcb.STORE_F16, 0),
+            (big, 1.0, mcb.G_POPULATIONS, mcb.STORE_F32, PAIR),
+            (big, 1.0, mcb.G_POPULATIONS, mcb.STORE_F16, PAIR),
+            (big, 0.8, mcb.G_AUTO, mcb.STORE_F32, 0),
+            (big, 0.8, mcb.G_AUTO, mcb.STORE_F16, PAIR + 1),
+            (big, 0.8, mcb.G_AUTO, mcb.STORE_BF16, PAIR + 1)):
+        cfg = mcb.default_config(nx=n[0], ny=n[1], nz=n[2], bc=mcb.BC_PERIODIC, tau_g=tau_g)
+        cfg.g_mode, cfg.storage = g_mode, storage
+        with mcb.Solver(cfg) as s:
+            assert s.schedule[0] == want, (n, tau_g, g_mode, storage)
+    cfg, phi, u = small_case(mcb.BC_PERIODIC, n=(47, 20, 30), tau_g=0.8)
+    cfg.storage = mcb.STORE_F16
     with mcb.Solver(cfg) as s:
         assert s.schedule[0] == 0
 
@@ -300,11 +317,41 @@ def test_pair_kernel_matches_the_one_cell_kernel(bc, storage):
         assert np.array_equal(runs[5][k], runs[6][k]), k  # the same arithmetic
 
 
-@pytest.mark.parametrize("bc,gravity,noise", [(mcb.BC_PERIODIC, 0.0, 0.0),
-                                              (mcb.BC_PERIODIC, 1e-4, 1e-3),
-                                              (mcb.BC_WALLS_Z, 1e-4, 1e-3)])
-def test_pair_kernel_matches_fp64_oracle(bc, gravity, noise):
-    cfg, phi, u = small_case(bc, gravity=gravity, noise=noise)
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
+@pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z])
+@pytest.mark.parametrize("g_form", ["relaxed", "populations"])
+def test_pair_kernel_with_stored_g_matches_the_one_cell_kernel(g_form, bc, storage):
+    """Stored g populations (relaxed with tau_g != 1, or stored at full relaxation): the
+    pair kernel on the blocked f layout against the one-cell kernel on the plain one. The
+    phi mass stays exact on both."""
+    cfg, phi, u = small_case(bc, n=(72, 22, 30), tau_g=0.8 if g_form == "relaxed" else 1.0,
+                             gravity=1e-4, noise=1e-3)
+    if g_form == "populations":
+        cfg.g_mode = mcb.G_POPULATIONS
+    cfg.storage = storage
+    runs = {}
+    for v in PAIRS + (0,):
+        cfg.variant = v
+        with mcb.Solver(cfg) as s:
+            s.set_fields(phi, *u)
+            assert s.schedule[0] == v
+            s.step(1)
+            m0 = s.diagnostics()["mass_q30"]
+            s.step(30)
+            runs[v] = {k: s.get(k).astype(np.float64) for k in FIELDS}
+            assert s.diagnostics()["mass_q30"] == m0, v
+    for k, tol in PAIR_TOL[storage].items():
+        assert maxdiff(runs[PAIR], runs[0], k) < tol, (k, maxdiff(runs[PAIR], runs[0], k))
+        assert np.array_equal(runs[5][k], runs[6][k]), k
+
+
+@pytest.mark.parametrize("bc,gravity,noise,tau_g", [(mcb.BC_PERIODIC, 0.0, 0.0, 1.0),
+                                                    (mcb.BC_PERIODIC, 1e-4, 1e-3, 1.0),
+                                                    (mcb.BC_WALLS_Z, 1e-4, 1e-3, 1.0),
+                                                    (mcb.BC_PERIODIC, 0.0, 1e-3, 0.8),
+                                                    (mcb.BC_WALLS_Z, 1e-4, 1e-3, 0.8)])
+def test_pair_kernel_matches_fp64_oracle(bc, gravity, noise, tau_g):
+    cfg, phi, u = small_case(bc, gravity=gravity, noise=noise, tau_g=tau_g)
     g = gpu_run(cfg, phi, u, steps=30, variant=PAIR)
     o = oracle_run(cfg, phi, u, steps=30)
     for k, tol in TOL.items():
@@ -326,12 +373,14 @@ def test_pair_kernel_in_reference_mode_matches_reference_kernels():
 
 
 def test_pair_kernel_is_skipped_where_it_does_not_apply():
-    # odd nx, stored relaxed g, D3Q27 f, a density ratio: the one-cell 32x8 tile runs
-    for over in ({"n": (23, 20, 28)}, {"tau_g": 0.8}, {"velocity_set": 27}, {"rho_in": 10.0}):
+    # odd nx, stored g populations in reference mode, D3Q27 f, a density ratio: the
+    # one-cell 32x8 tile runs
+    for over in ({"n": (23, 20, 28)}, {"g_mode": mcb.G_POPULATIONS, "bc": mcb.BC_REF},
+                 {"velocity_set": 27}, {"rho_in": 10.0}):
         kw = {k: v for k, v in over.items() if k in ("n", "tau_g")}
-        cfg, phi, u = small_case(mcb.BC_PERIODIC, **kw)
+        cfg, phi, u = small_case(over.get("bc", mcb.BC_PERIODIC), **kw)
         for k, v in over.items():
-            if k not in ("n", "tau_g"):
+            if k not in ("n", "tau_g", "bc"):
                 setattr(cfg, k, v)
         cfg.variant = PAIR
         with mcb.Solver(cfg) as s:
