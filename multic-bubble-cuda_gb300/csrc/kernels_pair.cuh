@@ -1,5 +1,7 @@
-// k_collide_pair: the equilibrium-g update of k_collide with two neighbouring cells in x per
-// thread, for D3Q19 f at density ratio 1 (the reference's model) on the blocked f layout.
+// k_collide_pair: the update of k_collide with two neighbouring cells in x per thread, for
+// D3Q19 f at density ratio 1 (the reference's model) on the blocked f layout, with every g
+// form (equilibrium g pushed; g populations stored, at full relaxation or relaxed with
+// tau_g != 1; the stored forms without the reference-mode shell).
 //
 // It computes what k_collide computes (gradCalc, curvatureCalc, momentiCalc, collisionFluid,
 // collisionPhase, streamingCalc and phiCalc of src/lbm.cu, fgBoundary and
@@ -12,8 +14,12 @@
 //     aligned 64-bit (FP32) or 32-bit (16-bit storage) load, and all 19 post-collision
 //     populations are stored for both cells with one such store each; 16-bit storage packs
 //     the pair with one conversion;
-//   - the 19 integer g populations of the two cells are summed per target before the shared
-//     atomics where their targets coincide (28 atomics for the pair instead of 38);
+//   - equilibrium g: the 19 integer g populations of the two cells are summed per target
+//     before the shared atomics where their targets coincide (28 atomics for the pair
+//     instead of 38);
+//   - relaxed g: the 18 pulled populations of a plane and their sources' previous phi are
+//     staged in shared memory by asynchronous copies one plane ahead (cp.async), so that no
+//     register holds them across the plane's barrier;
 //   - the per-plane and per-segment work (phi ring, offsets, loop) is shared by two cells.
 // Arithmetic and the exact integer push of phi are those of k_collide, so results agree with
 // it to FP32 rounding (the fused multiply-adds are placed explicitly here). Requires an even
