@@ -46,6 +46,36 @@ __device__ __forceinline__ float2 addsg(float2 b, float2 a) {
   else return sub(b, a);
 }
 
+// Sx x + Sy y + Sz z for compile-time signs in {-1, 0, 1}, starting from the first nonzero
+// term, which must be +1 (true of every odd population, the first of its opposite pair):
+// no add to a zero start, and the same value as that sum.
+template <int Sx, int Sy, int Sz>
+__device__ __forceinline__ float2 cdot(float2 x, float2 y, float2 z) {
+  if constexpr (Sx != 0) {
+    static_assert(Sx == 1, "the first term is positive");
+    float2 r = x;
+    if constexpr (Sy != 0) r = addsg<Sy>(r, y);
+    if constexpr (Sz != 0) r = addsg<Sz>(r, z);
+    return r;
+  } else if constexpr (Sy != 0) {
+    static_assert(Sy == 1, "the first term is positive");
+    return Sz != 0 ? addsg<Sz>(y, z) : y;
+  } else {
+    static_assert(Sz == 1, "the first term is positive");
+    return z;
+  }
+}
+// An accumulator's next term: the term itself when it is the first (kFirst; then Sg = +1).
+template <bool kFirst, int Sg>
+__device__ __forceinline__ float2 acc(float2 a, float2 v) {
+  if constexpr (kFirst) {
+    static_assert(Sg == 1, "the first term is positive");
+    return v;
+  } else {
+    return addsg<Sg>(a, v);
+  }
+}
+
 // Asynchronous B-byte copy (B = 4 or 8) from global to shared memory: the value goes
 // through no register, and cp_async_wait_all waits for this thread's copies.
 template <int B>
@@ -623,17 +653,22 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     };
     const float2 ncx = nrm2(n0, 0, 0), ncy = nrm2(n0, 1, 0), ncz = nrm2(n0, 2, 0);
     const float2 ncw = nrm2(n0, 3, 0);
+    // Per opposite pair (l, l + 1): W_l c_l . (n(x + c_l) - n(x - c_l)).
     float2 kap = dup(0.f);
-    static_for<1, kQ>([&](auto LC) {
-      constexpr int L = decltype(LC)::value;
+    static_for<0, (kQ - 1) / 2>([&](auto KC) {
+      constexpr int L = 2 * decltype(KC)::value + 1;
       constexpr float w3 = 3.0f * wf(L);
-      const float(*pl)[HP] = nbr_of<cz(L)>(nm, n0, np);
+      const float(*pp)[HP] = nbr_of<cz(L)>(nm, n0, np);   // x + c_l
+      const float(*pq)[HP] = nbr_of<-cz(L)>(nm, n0, np);  // x - c_l
       constexpr int o = cy(L) * HX + cx(L);
-      float2 cn = dup(0.f);
-      if constexpr (cx(L) != 0) cn = pk::addsg<cx(L)>(cn, nrm2(pl, 0, o));
-      if constexpr (cy(L) != 0) cn = pk::addsg<cy(L)>(cn, nrm2(pl, 1, o));
-      if constexpr (cz(L) != 0) cn = pk::addsg<cz(L)>(cn, nrm2(pl, 2, o));
-      kap = fma(dup(-w3), cn, kap);
+      const float2 cp = pk::cdot<cx(L), cy(L), cz(L)>(
+          cx(L) ? nrm2(pp, 0, o) : dup(0.f), cy(L) ? nrm2(pp, 1, o) : dup(0.f),
+          cz(L) ? nrm2(pp, 2, o) : dup(0.f));
+      const float2 cm = pk::cdot<cx(L), cy(L), cz(L)>(
+          cx(L) ? nrm2(pq, 0, -o) : dup(0.f), cy(L) ? nrm2(pq, 1, -o) : dup(0.f),
+          cz(L) ? nrm2(pq, 2, -o) : dup(0.f));
+      if constexpr (L == 1) kap = mul(dup(-w3), sub(cp, cm));
+      else kap = fma(dup(-w3), sub(cp, cm), kap);
     });
     const float2 phi = *reinterpret_cast<const float2*>(&sphi[slot5(z + 5)][(ty + 2) * PX + 2 * tx + 2]);
     const float2 mult = scale(kap, sigma);
@@ -644,7 +679,10 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
     // Moments (momentiCalc, src/lbm.cu:133-225), from opposite-pair sums; deviation storage
     // starts from the weights' moments.
     constexpr float m0 = kDevF ? 1.0f : 0.0f, m2 = kDevF ? 1.0f / 3.0f : 0.0f;
-    float2 rho = add(dup(m0), fval(std::integral_constant<int, 0>{}));
+    // Accumulators start from their first term (the first odd population with the component:
+    // x 1, y 3, z 5, xy 7, xz 9, yz 11, each with sign +1), not from an add to zero.
+    float2 rho = fval(std::integral_constant<int, 0>{});
+    if constexpr (kDevF) rho = add(dup(m0), rho);
     float2 jx = dup(0.f), jy = jx, jz = jx;
     float2 sxx = dup(m2), syy = sxx, szz = sxx, sxy = dup(0.f), sxz = sxy, syz = sxy;
     static_for<0, (QF - 1) / 2>([&](auto KC) {
@@ -653,12 +691,21 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
       const float2 fb = fval(std::integral_constant<int, L + 1>{});
       const float2 sp = add(fa, fb), dm = sub(fa, fb);
       rho = add(rho, sp);
-      if constexpr (cx(L) != 0) { jx = pk::addsg<cx(L)>(jx, dm); sxx = add(sxx, sp); }
-      if constexpr (cy(L) != 0) { jy = pk::addsg<cy(L)>(jy, dm); syy = add(syy, sp); }
-      if constexpr (cz(L) != 0) { jz = pk::addsg<cz(L)>(jz, dm); szz = add(szz, sp); }
-      if constexpr (cx(L) * cy(L) != 0) sxy = pk::addsg<cx(L) * cy(L)>(sxy, sp);
-      if constexpr (cx(L) * cz(L) != 0) sxz = pk::addsg<cx(L) * cz(L)>(sxz, sp);
-      if constexpr (cy(L) * cz(L) != 0) syz = pk::addsg<cy(L) * cz(L)>(syz, sp);
+      if constexpr (cx(L) != 0) {
+        jx = pk::acc<L == 1, cx(L)>(jx, dm);
+        sxx = pk::acc<!kDevF && L == 1, 1>(sxx, sp);
+      }
+      if constexpr (cy(L) != 0) {
+        jy = pk::acc<L == 3, cy(L)>(jy, dm);
+        syy = pk::acc<!kDevF && L == 3, 1>(syy, sp);
+      }
+      if constexpr (cz(L) != 0) {
+        jz = pk::acc<L == 5, cz(L)>(jz, dm);
+        szz = pk::acc<!kDevF && L == 5, 1>(szz, sp);
+      }
+      if constexpr (cx(L) * cy(L) != 0) sxy = pk::acc<L == 7, cx(L) * cy(L)>(sxy, sp);
+      if constexpr (cx(L) * cz(L) != 0) sxz = pk::acc<L == 9, cx(L) * cz(L)>(sxz, sp);
+      if constexpr (cy(L) * cz(L) != 0) syz = pk::acc<L == 11, cy(L) * cz(L)>(syz, sp);
     });
     const float2 inv_rho = make_float2(__frcp_rn(rho.x), __frcp_rn(rho.y));
     const float2 ux = mul(fma(dup(0.5f), Fx, jx), inv_rho);
@@ -772,10 +819,12 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
       constexpr int L = 2 * decltype(KC)::value + 1;
       constexpr int O = L + 1;
       constexpr float W = wf(L);
-      float2 cu = dup(0.f), cF = dup(0.f), qp = scale(tr3, -1.0f);
-      if constexpr (cx(L) != 0) { cu = pk::addsg<cx(L)>(cu, ux); cF = pk::addsg<cx(L)>(cF, Fx); qp = add(qp, pxx); }
-      if constexpr (cy(L) != 0) { cu = pk::addsg<cy(L)>(cu, uy); cF = pk::addsg<cy(L)>(cF, Fy); qp = add(qp, pyy); }
-      if constexpr (cz(L) != 0) { cu = pk::addsg<cz(L)>(cu, uz); cF = pk::addsg<cz(L)>(cF, Fz); qp = add(qp, pzz); }
+      const float2 cu = pk::cdot<cx(L), cy(L), cz(L)>(ux, uy, uz);
+      const float2 cF = pk::cdot<cx(L), cy(L), cz(L)>(Fx, Fy, Fz);
+      float2 qp = scale(tr3, -1.0f);
+      if constexpr (cx(L) != 0) qp = add(qp, pxx);
+      if constexpr (cy(L) != 0) qp = add(qp, pyy);
+      if constexpr (cz(L) != 0) qp = add(qp, pzz);
       if constexpr (cx(L) * cy(L) != 0) qp = fma(dup(2.0f * cx(L) * cy(L)), pxy, qp);
       if constexpr (cx(L) * cz(L) != 0) qp = fma(dup(2.0f * cx(L) * cz(L)), pxz, qp);
       if constexpr (cy(L) * cz(L) != 0) qp = fma(dup(2.0f * cy(L) * cz(L)), pyz, qp);
@@ -792,10 +841,8 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
         constexpr int L = 2 * decltype(KC)::value + 1;
         constexpr int O = L + 1;
         constexpr float WG = wf(L);
-        float2 cu = dup(0.f), cn = dup(0.f);
-        if constexpr (cx(L) != 0) { cu = pk::addsg<cx(L)>(cu, ux); cn = pk::addsg<cx(L)>(cn, ncx); }
-        if constexpr (cy(L) != 0) { cu = pk::addsg<cy(L)>(cu, uy); cn = pk::addsg<cy(L)>(cn, ncy); }
-        if constexpr (cz(L) != 0) { cu = pk::addsg<cz(L)>(cu, uz); cn = pk::addsg<cz(L)>(cn, ncz); }
+        const float2 cu = pk::cdot<cx(L), cy(L), cz(L)>(ux, uy, uz);
+        const float2 cn = pk::cdot<cx(L), cy(L), cz(L)>(ncx, ncy, ncz);
         const float2 dg = fma(phi3, cu, mul(A, cn));
         float2 gL = scale(add(phi, dg), WG), gO = scale(sub(phi, dg), WG);
         if constexpr (BGK) {

@@ -278,14 +278,16 @@ def test_work_splits_agree_bitwise_with_equilibrium_g(storage):
 
 
 # |pair kernel - one-cell kernel| after 31 updates. FP32: the same arithmetic with the fused
-# multiply-adds placed differently, so the fields part at FP32 rounding (the FP32 and FP64
-# oracles part by 5e-7 in phi and 1e-6 in rho on these cases). 16-bit storage rounds every
-# stored population, and a last-bit difference before the rounding moves it by one 16-bit
-# unit: the bounds are those of the storage itself (measured: FP16 2.1e-5 in rho and 6.4e-6
-# in u, BF16 5.1e-5 in u).
-PAIR_TOL = {mcb.STORE_F32: {"phi": 2e-6, "rho": 4e-6, "ux": 4e-7, "uy": 4e-7, "uz": 4e-7},
+# multiply-adds placed differently and the curvature summed per opposite pair, so the fields
+# part at FP32 rounding (the FP32 and FP64 oracles part by 5e-7 in phi and 1e-6 in rho on
+# these cases; the reference-mode case, whose shell amplifies rounding, parts by 3.0e-6 in
+# phi). 16-bit storage rounds every stored population, and a last-bit difference before the
+# rounding moves it by one 16-bit unit: the bounds are those of the storage itself (measured:
+# FP16 2.1e-5 in rho and 6.4e-6 in u, BF16 5.1e-5 in u; BF16 in reference mode 1.03e-3 in
+# phi, where the shell amplifies those units).
+PAIR_TOL = {mcb.STORE_F32: {"phi": 5e-6, "rho": 4e-6, "ux": 4e-7, "uy": 4e-7, "uz": 4e-7},
             mcb.STORE_F16: {"phi": 2e-4, "rho": 2e-4, "ux": 4e-5, "uy": 4e-5, "uz": 4e-5},
-            mcb.STORE_BF16: {"phi": 1e-3, "rho": 1e-3, "ux": 2e-4, "uy": 2e-4, "uz": 2e-4}}
+            mcb.STORE_BF16: {"phi": 2e-3, "rho": 1e-3, "ux": 2e-4, "uy": 2e-4, "uz": 2e-4}}
 
 
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16, mcb.STORE_BF16])
@@ -453,6 +455,33 @@ def test_batch_matches_single_cases_bitwise():
 
 
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
+def test_batch_with_relaxed_g_on_the_pair_kernel_matches_single_cases_bitwise(storage):
+    """Stored, relaxed g on the pair kernel in one launch over uneven cases: the staged
+    pulls and the push address each case's own g and phi arrays."""
+    cases = []
+    for i, (n, bc) in enumerate([((16, 16, 16), mcb.BC_PERIODIC), ((24, 20, 28), mcb.BC_WALLS_Z),
+                                 ((72, 22, 30), mcb.BC_PERIODIC)]):
+        cfg, phi, u = small_case(bc, n=n, tau_g=0.8, noise=1e-3, seed=i,
+                                 gravity=1e-4 * (i == 1))
+        cfg.storage = storage
+        cfg.tau = 0.6 + 0.1 * i
+        cfg.variant = PAIR
+        cases.append((cfg, phi, u))
+    with mcb.Batch([c for c, _, _ in cases]) as b:
+        for i, (c, phi, u) in enumerate(cases):
+            b.set_fields(i, phi, *u)
+            assert b.schedule(i)[0] == PAIR
+        b.step(33)
+        got = [{k: b.get(i, k) for k in FIELDS} for i in range(len(cases))]
+        dg = [b.diagnostics(i) for i in range(len(cases))]
+    for i, (c, phi, u) in enumerate(cases):
+        single = gpu_run(c, phi, u, steps=33)
+        for k in FIELDS:
+            assert np.array_equal(got[i][k].astype(np.float64), single[k]), (i, k)
+        assert dg[i]["mass_q30"] == single["diag"]["mass_q30"]
+
+
+@pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
 @pytest.mark.parametrize("bc", [mcb.BC_PERIODIC, mcb.BC_WALLS_Z, mcb.BC_REF])
 def test_equilibrium_g_storage_matches_stored_populations(bc, storage):
     """With tau_g = 1 the solver stores J instead of the 19 g populations (g_mode auto).
@@ -554,14 +583,18 @@ def test_autotune_restores_the_state(tau_g, storage):
 
 
 @pytest.mark.parametrize("storage", [mcb.STORE_F32, mcb.STORE_F16])
-@pytest.mark.parametrize("bc,tau_g", [(mcb.BC_PERIODIC, 1.0), (mcb.BC_WALLS_Z, 0.8),
-                                      (mcb.BC_REF, 1.0)])
-def test_checkpoint_restart_continues_bitwise(tmp_path, bc, tau_g, storage):
+@pytest.mark.parametrize("bc,tau_g,variant", [(mcb.BC_PERIODIC, 1.0, -1),
+                                              (mcb.BC_WALLS_Z, 0.8, -1),
+                                              (mcb.BC_WALLS_Z, 0.8, PAIR + 1),
+                                              (mcb.BC_REF, 1.0, -1)])
+def test_checkpoint_restart_continues_bitwise(tmp_path, bc, tau_g, variant, storage):
+    """Default tiles, and relaxed g on the pair kernel (blocked f layout, stored g)."""
     if bc == mcb.BC_REF:
         cfg, phi, u = reference_cfg(32), off_centre_reference_phi(32), None
     else:
         cfg, phi, u = small_case(bc, tau_g=tau_g, gravity=1e-4, noise=1e-3)
     cfg.storage = storage
+    cfg.variant = variant
     ck = str(tmp_path / "state.ckpt")
     with mcb.Solver(cfg) as s:
         s.set_fields(phi, *(u if u is not None else (None, None, None)))
@@ -571,6 +604,8 @@ def test_checkpoint_restart_continues_bitwise(tmp_path, bc, tau_g, storage):
         want = {k: s.get(k) for k in FIELDS}
         want_d = s.diagnostics()
     with mcb.Solver(cfg) as s2:
+        if variant >= 0:
+            assert s2.schedule[0] == variant
         s2.checkpoint_load(ck)
         assert s2.update == 30
         s2.step(23)
