@@ -204,8 +204,13 @@ int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_s
 
 /* The tile variant and z chunk setting the handle runs (after defaults and autotuning).
  * variant 4 is the TMA-staged 32x8 collide on the padded f layout; variant 5 takes two
- * neighbouring cells in x per thread (64x4 cells per block, equilibrium g with D3Q19 f at
- * density ratio 1 and an even nx; elsewhere a request for it runs variant 0). */
+ * neighbouring cells in x per thread (64x4 cells per block; D3Q19 f at density ratio 1 and
+ * an even nx; with stored g also periodic or wall boundaries and 18 * cells < 2^31;
+ * elsewhere a request for it runs variant 0), and variant 6 is variant 5 with an L2
+ * prefetch of the f rows of the plane after next. Defaults: variant 5 where it applies,
+ * except with stored g below 2^21 cells (variant 0) and relaxed g (tau_g != 1: variant 6 at
+ * 16-bit storage, variant 0 at FP32). With stored g the f layout follows the variant chosen
+ * at creation: the autotuner then tries variants 5 and 6, or the one-cell ones, only. */
 int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
 
 /* Checkpoint and restart. No counterpart in the reference, which saves only phi
@@ -218,8 +223,10 @@ int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
  *   - the fields of the latest update;
  *   - the update counter, the buffer parity and the buoyancy reference;
  * together with the configuration. mcb_checkpoint_load restores them into a handle created
- * with the same size, boundary mode, storage and g mode (MCB_ERR_INVALID otherwise). The
- * run then continues bit-identically. The file is raw little-endian. */
+ * with the same size, boundary mode, storage, g mode and f layout (MCB_ERR_INVALID
+ * otherwise; the layout differs between the pair variants and the others with stored g,
+ * and for the TMA variant). The run then continues bit-identically. The file is raw
+ * little-endian. */
 int  mcb_checkpoint_save(mcb_handle* h, const char* path);
 int  mcb_checkpoint_load(mcb_handle* h, const char* path);
 

@@ -255,7 +255,10 @@ struct Solver {
       // that the whole case is one wave whose blocks march neighbouring columns in step
       // (128x128x256: 37 planes, 2 % faster than 16-plane chunks, 2.4 % faster than
       // balanced runs at FP32). Otherwise 32-plane chunks (512^3: 13 % faster than balanced
-      // runs, 2.5 % faster than 16), keeping at least 8 planes per chunk.
+      // runs, 2.5 % faster than 16). A chunk keeps at least 4 planes: on the 64^3 static
+      // bubble 4-plane chunks (256 blocks) run 20.6 us per update against 25.2 with 8 and
+      // 23.6 with 2 (FP32, relaxed g), 14.6 against 17.6 with 8 (FP16, pair kernel,
+      // equilibrium g).
       const long long wave = 1LL * occ_col * nsm;
       long long cols = 0;
       int nzmax = 1;
@@ -264,7 +267,7 @@ struct Solver {
         nzmax = std::max(nzmax, cases[ci].nz);
       }
       if (g.members.size() == 1 && cols <= wave) {
-        const long long m = std::max<long long>(1, std::min<long long>(wave / cols, nzmax / 8));
+        const long long m = std::max<long long>(1, std::min<long long>(wave / cols, nzmax / 4));
         zc = static_cast<int>((nzmax + m - 1) / m);
       } else {
         zc = 32;

@@ -619,6 +619,12 @@ def test_checkpoint_restart_continues_bitwise(tmp_path, bc, tau_g, variant, stor
         with pytest.raises(mcb.McbError) as e:
             s3.checkpoint_load(ck)
         assert e.value.code == mcb.ERR_INVALID
+    if variant >= 0:  # stored g on the pair kernel's blocked f: not loadable into plain f
+        cfg.variant = 0
+        with mcb.Solver(cfg) as s4:
+            with pytest.raises(mcb.McbError) as e:
+                s4.checkpoint_load(ck)
+            assert e.value.code == mcb.ERR_INVALID
 
 
 def test_errors_come_back_as_status_codes():
