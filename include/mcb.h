@@ -207,9 +207,10 @@ int  mcb_write_info_file(const char* dir, const char* id, const char* velocity_s
  * neighbouring cells in x per thread (64x4 cells per block; D3Q19 f at density ratio 1 and
  * an even nx; with stored g also periodic or wall boundaries and 18 * cells < 2^31;
  * elsewhere a request for it runs variant 0), and variant 6 is variant 5 with an L2
- * prefetch of the f rows of the plane after next. Defaults: variant 5 where it applies,
- * except with stored g below 2^21 cells (variant 0) and relaxed g (tau_g != 1: variant 6 at
- * 16-bit storage, variant 0 at FP32). With stored g the f layout follows the variant chosen
+ * prefetch of the f rows of the plane after next. Defaults: variant 5 where it applies
+ * and its 64-cell-wide tiles are at least 85 % as full in x as 32-wide ones, except with
+ * stored g below 2^18 cells (variant 0) and relaxed g (tau_g != 1: variant 6 at 16-bit
+ * storage, variant 0 at FP32). With stored g the f layout follows the variant chosen
  * at creation: the autotuner then tries variants 5 and 6, or the one-cell ones, only. */
 int  mcb_get_schedule(const mcb_handle* h, int* variant, int* zchunk);
 

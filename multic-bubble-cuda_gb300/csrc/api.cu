@@ -438,13 +438,26 @@ struct Solver {
     //   - g stored at full relaxation: 163 / 147 / 156 us against 174 / 171 / 198;
     //   - relaxed g (tau_g 0.8): 16-bit storage with the L2 prefetch variant, 275 / 303 us
     //     against 298 / 313; at FP32 the one-cell tile stays (233 us against 286).
-    // Stored g takes the pair kernel from 2^21 cells: its blocks hold half the threads of
-    // the one-cell tile's, and the 64^3 static bubble (relaxed g) runs 47 / 52 us there
-    // against 39 / 41 one cell per thread at 16-bit storage.
-    if (cs[0].variant < 0 && pair_ok) {
+    // Where nx leaves the pair kernel's 64-cell-wide tiles emptier than the one-cell
+    // kernel's 32-wide ones, the one-cell tile stays: 96^3, equilibrium g, 35.6 us against
+    // 41.0 (FP32); 80^3 27.9 against 31.9. 200x200x100 (tiles 78 % full, against 89 %)
+    // still runs the pair kernel faster, 157 us against 175. Stored g takes the pair kernel
+    // from 64^3 (there 16.6 us against 17.8 for the populations at FP32, 25.1 against 26.0
+    // relaxed at FP16); 32^3 and 96^3 run faster one cell per thread.
+    auto x_fill = [&](int w) {  // share of the tiles' thread columns that hold cells
+      double c = 0, t = 0;
+      for (auto& d : cases) {
+        c += static_cast<double>(d.nx) * d.ny * d.nz;
+        t += static_cast<double>((d.nx + w - 1) / w) * w * d.ny * d.nz;
+      }
+      return c / t;
+    };
+    const bool pair_fills = x_fill(mcb::kVariants[mcb::kPairVariant].bx) >=
+                            0.85 * x_fill(mcb::kVariants[0].bx);
+    if (cs[0].variant < 0 && pair_ok && pair_fills) {
       if (gmode == mcb::kGEquil) variant = mcb::kPairVariant;
-      else if (cells_total >= (1LL << 21) && gmode == mcb::kGPop) variant = mcb::kPairVariant;
-      else if (cells_total >= (1LL << 21) && storage != MCB_STORE_F32)
+      else if (cells_total >= (1LL << 18) && gmode == mcb::kGPop) variant = mcb::kPairVariant;
+      else if (cells_total >= (1LL << 18) && storage != MCB_STORE_F32)
         variant = mcb::kPairVariant + 1;
     }
     // f layout: blocked with equilibrium g and 32-bit offsets (x rounded up to whole 32-cell

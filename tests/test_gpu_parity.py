@@ -233,12 +233,14 @@ def test_tma_collide_is_skipped_where_it_does_not_apply():
     cfg.variant = 4
     with mcb.Solver(cfg) as s:
         assert s.schedule[0] == 0
-    # The default is the two-cells-per-thread tile where it applies, else the 32x8 tile.
-    # Stored g takes it from 2^21 cells (relaxed g: with the L2 prefetch at 16-bit storage,
-    # not at all at FP32).
-    big = (128, 128, 128)
+    # The default is the two-cells-per-thread tile where it applies and its 64-wide tiles
+    # fill x nearly as well as 32-wide ones, else the 32x8 tile. Stored g takes it from 2^18
+    # cells (relaxed g: with the L2 prefetch at 16-bit storage, not at all at FP32).
+    big = (64, 64, 64)
     for n, tau_g, g_mode, storage, want in (
             ((48, 20, 30), 1.0, mcb.G_AUTO, mcb.STORE_F32, PAIR),
+            ((96, 20, 30), 1.0, mcb.G_AUTO, mcb.STORE_F32, 0),
+            ((200, 20, 30), 1.0, mcb.G_AUTO, mcb.STORE_F16, PAIR),
             ((48, 20, 30), 1.0, mcb.G_POPULATIONS, mcb.STORE_F16, 0),
             ((48, 20, 30), 0.8, mcb.G_AUTO, mcb.STORE_F16, 0),
             (big, 1.0, mcb.G_POPULATIONS, mcb.STORE_F32, PAIR),
