@@ -347,23 +347,25 @@ def reference_mode_run(device, steps, nx=128, ny=128, nz=256, tau=0.7, sigma=0.0
             "k_collide_ms": t_col / steps}
 
 
-def reference_cuda_stock(device, steps):
+def reference_cuda_stock(device, steps, nx=64, ny=64, nz=256, tau=0.505, sigma=0.1,
+                         sharp_c=0.45, r=20.0, width=3.0, label="stock constants"):
     """The reference's own kernels at the reference's stock setting: 64x64x256, tau 0.505,
-    sigma 0.1, SHARP_C 0.45 (src/var.cu:3-25), R 20 and width 3 (src/init.cu:39,46)."""
+    sigma 0.1, SHARP_C 0.45 (src/var.cu:3-25), R 20 and width 3 (src/init.cu:39,46); or at
+    another size and setting (the static bubble: 64^3, tau 0.8, sigma 0.1, SHARP_C 0.5, R 12,
+    width 4)."""
     from oracle.oracle import ReferenceKernels, harness_available
     import mcb
 
     if not harness_available():
         return {"unavailable": "reference cubin not present"}
-    nx, ny, nz = 64, 64, 256
-    phi = mcb.fill_phi_reference(nx, ny, nz, 20.0, 3.0)
-    rk = ReferenceKernels(nx, ny, nz, 0.505, 0.1, 0.45, device=device)
+    phi = mcb.fill_phi_reference(nx, ny, nz, r, width)
+    rk = ReferenceKernels(nx, ny, nz, tau, sigma, sharp_c, device=device)
     rk.set_phi(phi)
     rk.run(5)
     ms = rk.run(steps)
     rk.close()
     return {"value": nx * ny * nz * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS",
-            "config": "64x64x256 stock constants, one stream, 10 launches per update",
+            "config": f"{nx}x{ny}x{nz} {label}, one stream, 10 launches per update",
             "steps": steps}
 
 
@@ -719,6 +721,14 @@ def main():
             mine_stock["ratio_vs_reference_cuda"] = mine_stock["value"] / stock["value"]
         result["reference_cuda_stock"] = stock
         result["reference_mode_stock"] = mine_stock
+        # the static bubble (64^3, the reference's frozen shell at tau 0.8, sigma 0.1)
+        sb = reference_cuda_stock(local, nref, 64, 64, 64, 0.8, 0.1, 0.5, 12.0, 4.0,
+                                  "static bubble R 12, tau 0.8, sigma 0.1, SHARP_C 0.5")
+        mine_sb = reference_mode_run(local, nref, 64, 64, 64, 0.8, 0.1, 12.0, 4.0, 0.5)
+        if "value" in sb:
+            mine_sb["ratio_vs_reference_cuda"] = mine_sb["value"] / sb["value"]
+        result["reference_cuda_static_bubble"] = sb
+        result["reference_mode_static_bubble"] = mine_sb
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
         print(json.dumps(result))
     barrier(dist)
