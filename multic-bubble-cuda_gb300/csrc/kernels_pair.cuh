@@ -477,7 +477,9 @@ __device__ __forceinline__ void collide_pair_segment(const StepArgs& a, const Ti
   int* const pring = reinterpret_cast<int*>(pair_dyn + pair_gbuf_bytes<S>());
   // A staged coordinate one step or so past the lattice edge, wrapped (the reads that use
   // it); coordinates further out are never read and take 0.
-  auto wrap_st = [](int v, int n) { return v < 0 ? v + n : (v < n ? v : (v - n < n ? v - n : 0)); };
+  auto wrap_st = [](int v, int n) {
+    return v < 0 ? v + n : (v < n ? v : (v - n < n ? v - n : 0));
+  };
   constexpr int KPJ = (PR * GW + NT - 1) / NT;  // previous-phi words per thread and plane
   auto gplane = [&](int q) {  // the stored plane of plane index q (walls: clamped, unread)
     if (t.bc == kBcPeriodic) q = wrap1(q, nz);
